@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark of the differentiable confocal mesh render (forward + backward).
+
+Workload (the headline differentiable configuration): level-5 icosphere
+(20,480 faces) with 0.05 m low-frequency radial displacement, 64x64 confocal
+scan on [-1,1]^2, 1,024 bins of 0.005 m, visibility on, MSE loss against a
+target transient rendered from a second seeded mesh; gradients with respect to
+vertex positions and albedo. One step = forward render + loss + backward
+through ``totri_gb300.render.MeshRenderConfocal``. Unit of work: one
+(scan point, face) pair; 83,886,080 pairs per step.
+
+Prints one JSON line. ``--impl reference`` times the CPU restatement of the
+reference algorithm (oracle/) on the host cores instead (the reference's
+mesh path needs the OptiX SDK and cannot be built).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "mesh fwd+bwd scanpt·tri pairs/s"
+UNIT = "pairs/s"
+WORKLOAD = ("confocal mesh fwd+bwd: level-5 icosphere 20480 faces, radial SH displacement "
+            "0.05 m, 64x64 scan, 1024 bins x 0.005 m, visibility on, MSE vs target mesh")
+# FLOP model per (scan point, face) pair: add/mul = 1, FMA = 2, div/sqrt/exp = 1.
+FLOP_SPLAT = 116.0       # forward geometry, alpha, bins
+FLOP_GRAD = 190.0        # backward recomputation + alpha log-derivative
+FLOP_PER_SEG_FWD = 10.0  # per bin segment of the tent (forward)
+FLOP_PER_SEG_BWD = 60.0  # per bin segment (backward)
+
+
+def flop_visibility(num_faces):
+    """Per-ray BVH visibility model: 2 box tests x 20 per level + 4 triangle tests x 36."""
+    return 40.0 * math.ceil(math.log2(max(num_faces, 2))) + 144.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=None)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# Distributed helpers (one process per GPU; replicas, no data-path collective).
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not torch.distributed.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        torch.distributed.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region.
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# Workload.
+
+def make_workload(device):
+    from totri_gb300 import scenes
+    from totri_gb300.render import MeshRenderConfocal
+    s = scenes.confocal_differentiable()
+    bd = s["bin_def"]
+    w = {k: (v.to(device) if torch.is_tensor(v) else v) for k, v in s.items()}
+    with torch.no_grad():
+        target = MeshRenderConfocal.apply(w["target_verts"], w["faces"], w["scan_points"], bd,
+                                          w["target_colors"])
+    w["target"] = target.contiguous()
+    w["host"] = s
+    return w
+
+
+def step(w, verts, colors, faces, scan_points, target):
+    from totri_gb300.render import MeshRenderConfocal
+    verts = verts.detach().requires_grad_(True)
+    colors = colors.detach().requires_grad_(True)
+    tr = MeshRenderConfocal.apply(verts, faces, scan_points, w["bin_def"], colors)
+    loss = torch.mean((tr - target) ** 2)
+    loss.backward()
+    return loss, verts.grad, colors.grad
+
+
+def mean_segments(w, device, stride=8):
+    """b-bar: mean bin count of the tent per (scan point, face) pair, 0 for pairs
+    that are occluded or out of range (computed on a 1/stride scan subset)."""
+    from totri_gb300.totri_cpp import render as R
+    verts, faces, sp = w["verts"], w["faces"], w["scan_points"][:, ::stride].contiguous()
+    bd = w["bin_def"]
+    F = faces.shape[1]
+    mask = R.mesh_visibility(verts, faces, sp)[0]
+    bits = ((mask.unsqueeze(-1) >> torch.arange(32, device=device, dtype=torch.int32)) & 1)
+    vis = bits.reshape(mask.shape[0], -1)[:, :F].bool()
+    tri = verts[0][faces[0].long()]                         # [F, 3, 3]
+    d = torch.linalg.norm(tri[None] - sp[0][:, None, None, :], dim=-1)  # [S', F, 3]
+    c = (2.0 * d - bd.offset) / bd.width
+    lo = c.min(dim=-1).values.floor()
+    hi = c.max(dim=-1).values.floor().clamp(max=bd.num - 1)
+    seg = (hi - lo.clamp(min=0) + 1).clamp(min=0)
+    seg = torch.where(vis & (lo < bd.num), seg, torch.zeros_like(seg))
+    return float(seg.mean())
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restatement on the host cores).
+
+def cpu_baseline(w_host, scan_subset):
+    import oracle
+    v = w_host["verts"][0].numpy()
+    f = w_host["faces"][0].numpy()
+    c = w_host["colors"][0].numpy()
+    sp = w_host["scan_points"][0].numpy()[scan_subset]
+    bd = w_host["bin_def"]
+    oracle.lib()
+    t0 = time.perf_counter()
+    vis = oracle.mesh_visibility(v, f, sp, bvh=True)
+    tr = oracle.mesh_confocal_forward(v, f, c, sp, None, vis, bd.num, bd.width, bd.offset,
+                                      fp64=False)
+    g = 2.0 * tr / tr.size
+    oracle.mesh_confocal_grad(v, f, c, sp, None, vis, bd.num, bd.width, bd.offset, g,
+                              fp64=False)
+    dt = time.perf_counter() - t0
+    pairs = sp.shape[0] * f.shape[0]
+    return pairs / dt, dt, pairs
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from totri_gb300 import scenes
+    s = scenes.confocal_differentiable()
+    S = s["scan_points"].shape[1]
+    n_sub = 64
+    subset = np.linspace(0, S - 1, n_sub).round().astype(np.int64)
+    for _ in range(args.warmup):
+        cpu_baseline(s, subset[:8])
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, dt, pairs = cpu_baseline(s, subset)
+        rates.append(r)
+        times.append(dt)
+    value = float(np.median(rates))
+    total_pairs = S * s["faces"].shape[1]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_pairs / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "faces": int(s["faces"].shape[1]), "scan_points": S,
+                   "bins": s["bin_def"].num},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                         "sample": "%d of %d scan points x all faces per step (BVH visibility, "
+                                   "forward, gradient; FP32; OpenMP)" % (n_sub, S)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference mesh path needs the OptiX SDK (absent); this arm runs the "
+                "CPU restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        # rank 0 alone times the CPU restatement; other ranks exit without work
+        run_reference(args, int(os.environ.get("WORLD_SIZE", "1")),
+                      int(os.environ.get("RANK", "0")))
+        return
+    world, rank, local = dist_setup()
+    from totri_gb300 import _lib
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    _lib.load()
+    w = make_workload(device)
+    S, F = w["scan_points"].shape[1], w["faces"].shape[1]
+    pairs = S * F
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    for _ in range(max(args.warmup, 3)):
+        step(w, w["verts"], w["colors"], w["faces"], w["scan_points"], w["target"])
+    torch.cuda.synchronize(device)
+
+    # Device-timed region: inputs resident, L2 flushed between steps.
+    clocks = ClockSampler(device.index)
+    clocks.start()
+    _lib.profile_reset()
+    _lib.profile_enable(True)
+    barrier(world)
+    torch.cuda.synchronize(device)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(w, w["verts"], w["colors"], w["faces"], w["scan_points"], w["target"])
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize(device)
+    barrier(world)
+    _lib.profile_enable(False)
+    prof = _lib.profile_read()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(total_ms, world, device)
+    ms_per_step = total_ms / args.steps
+    value = world * pairs * args.steps / (total_ms / 1000.0)
+    launches = sum(v[0] for v in prof.values())
+
+    # Roofline of the dominant kernel (FP32 SIMT: no tensor-core work exists here).
+    bbar = mean_segments(w, device)
+    flops = {
+        "mesh visibility": flop_visibility(F),
+        "mesh confocal splat": FLOP_SPLAT + FLOP_PER_SEG_FWD * bbar,
+        "mesh confocal grad": FLOP_GRAD + FLOP_PER_SEG_BWD * bbar,
+    }
+    dom = max(prof.items(), key=lambda kv: kv[1][2])
+    dom_name, (dom_launches, dom_timed, dom_ms) = dom
+    peaks = measured_peaks()
+    sm_count = torch.cuda.get_device_properties(device).multi_processor_count
+    max_mhz = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sm_count * 128 * 2 * max_mhz * 1e6 / 1e12
+    roof = None
+    if dom_name in flops and dom_timed > 0:
+        per_launch_ms = dom_ms / dom_timed
+        achieved = pairs * flops[dom_name] / (per_launch_ms / 1000.0) / 1e12
+        traffic = load_traffic().get(dom_name)
+        roof = {"bound": "fp32", "kernel": dom_name, "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                "peak_source": "nominal FP32 SIMT: %d SMs x 128 lanes x 2 FLOP x %.0f MHz "
+                               "(MEASURED_PEAKS.json holds no FP32 figure)" % (sm_count, max_mhz),
+                "flop_per_pair": flops[dom_name], "pairs_per_launch": pairs,
+                "ms_per_launch": per_launch_ms, "b_bar": bbar}
+    kernels = {k: {"launches": v[0], "ms_per_step": v[2] / args.steps} for k, v in prof.items()}
+
+    # End to end through the public API with host buffers.
+    h = w["host"]
+    pin = {k: h[k].pin_memory() for k in ("verts", "faces", "colors", "scan_points")}
+    pin["target"] = w["target"].cpu().pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in pin.values())
+    out_loss = torch.empty((), dtype=torch.float32).pin_memory()
+    out_vg = torch.empty_like(pin["verts"]).pin_memory()
+    out_cg = torch.empty_like(pin["colors"]).pin_memory()
+    d2h = 4 + out_vg.numel() * 4 + out_cg.numel() * 4
+    e2e_steps = args.e2e_steps or args.steps
+    for it in range(2 + e2e_steps):
+        if it == 2:
+            torch.cuda.synchronize(device)
+            barrier(world)
+            t0 = time.perf_counter()
+        d = {k: v.to(device, non_blocking=True) for k, v in pin.items()}
+        loss, vg, cg = step(w, d["verts"], d["colors"], d["faces"], d["scan_points"],
+                            d["target"])
+        out_loss.copy_(loss.detach(), non_blocking=True)
+        out_vg.copy_(vg, non_blocking=True)
+        out_cg.copy_(cg, non_blocking=True)
+        torch.cuda.synchronize(device)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, device)
+    e2e_value = world * pairs * e2e_steps / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        subset = np.linspace(0, S - 1, 64).round().astype(np.int64)
+        cpu_baseline(h, subset[:4])
+        rate, dt, n = cpu_baseline(h, subset)
+        cpu = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+               "sample": "64 of 4096 scan points x 20480 faces (%d pairs, %.1f s): BVH "
+                         "visibility + forward + gradient, FP32, OpenMP" % (n, dt)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "faces": F, "scan_points": S,
+                       "bins": w["bin_def"].num, "pairs_per_step": pairs,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between timed steps (256 MiB memset)"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "clocks": clk, "gpu_launches": launches, "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,320 @@
+/*
+ * totri_gb300 C ABI: GB300-native (sm_103a) transient rendering, backprojection
+ * and RBF-to-volume kernels of totrilib behind plain C entry points.
+ *
+ * Every entry point replaces one function of the reference's pybind11 module
+ * `totri_cpp` (src/totri.cpp:13-54) with the same argument order and tensor
+ * layouts. Tensors cross the boundary as `totri_array_t` descriptors (device
+ * pointer, dtype, shape, strides in elements) instead of at::Tensor; scalars
+ * keep their reference types. Nothing here allocates device memory: callers
+ * query the scratch size with the matching *_workspace() function and pass a
+ * device buffer of at least that many bytes (NULL when the size is 0).
+ * Kernels are enqueued on `stream` (a cudaStream_t) and the call returns
+ * without synchronising. All functions return TOTRI_OK (0) or an error code;
+ * totri_last_error() describes the last failure on the calling thread.
+ *
+ * Layout rules: small per-point/per-vertex arrays (verts, faces, material,
+ * points, origins, rbf parameters) accept arbitrary strides (including 0 for
+ * broadcast dimensions, as produced by torch expand()); dense outputs and
+ * dense gradients (transients, volumes) must be C-contiguous.
+ */
+#ifndef TOTRI_GB300_H
+#define TOTRI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------- */
+/* Status codes, dtypes, descriptors                                        */
+
+enum totri_status {
+  TOTRI_OK = 0,
+  TOTRI_ERR_INVALID_ARGUMENT = 1, /* bad shape/dtype/stride (ValueError)   */
+  TOTRI_ERR_WORKSPACE = 2,        /* workspace missing or too small         */
+  TOTRI_ERR_CUDA = 3,             /* a CUDA runtime call failed             */
+  TOTRI_ERR_UNSUPPORTED = 4,      /* valid in the reference, not supported  */
+  TOTRI_ERR_DEVICE = 5            /* a kernel reported an error status     */
+};
+
+enum totri_dtype {
+  TOTRI_FLOAT32 = 0,
+  TOTRI_FLOAT64 = 1,
+  TOTRI_INT32 = 2,
+  TOTRI_INT64 = 3
+};
+
+#define TOTRI_MAX_DIMS 5
+
+typedef struct totri_array {
+  void* data;                       /* device pointer (may be NULL if numel 0) */
+  int32_t dtype;                    /* enum totri_dtype                         */
+  int32_t ndim;                     /* number of dimensions (<= 5)              */
+  int64_t shape[TOTRI_MAX_DIMS];    /* sizes                                    */
+  int64_t strides[TOTRI_MAX_DIMS];  /* strides in elements                      */
+} totri_array_t;
+
+/* Library version string. */
+const char* totri_version(void);
+/* Message describing the last failure on the calling thread ("" if none). */
+const char* totri_last_error(void);
+
+/* Launch accounting (no reference counterpart). Every kernel launch is
+ * counted per kernel name; while enabled, launches are also bracketed by CUDA
+ * events on their stream. totri_profile_read synchronises on those events and
+ * reports, per kernel name (64-byte NUL-terminated slots in `names`), the
+ * launches since the last reset, how many of them were timed, and their total
+ * device time in milliseconds. */
+int totri_profile_enable(int on);
+void totri_profile_reset(void);
+int totri_profile_read(int max_entries, char* names, int64_t* launches, int64_t* timed,
+                       double* total_ms, int* n_entries);
+
+/* ----------------------------------------------------------------------- */
+/* render: meshes                                                           */
+
+/* Scratch bytes for the mesh entry points: one BVH, one visibility mask per
+ * batch item. num_points is S (confocal) or S + L (exhaustive). */
+size_t totri_mesh_workspace(int64_t batch, int64_t num_verts, int64_t num_faces,
+                            int64_t num_points);
+
+/* Replaces totri_cpp.render.mesh_confocal_forward
+ * (src/render/mesh.h:10-18, src/render/mesh.cpp:9-20).
+ * verts [B,V,3] f32, faces [B|1,F,3] i32/i64 (-1 padded: the first face with a
+ * negative index ends the list), material [B,V,M] f32 (M<=4, M==0 -> albedo 1),
+ * scan_points [B,S,3] f32, scan_origin [B,S,3] or [B,0,3] f32,
+ * transient [B,T,S] f32 (written, not accumulated). `model` is ignored, as in
+ * the reference. */
+int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                const totri_array_t* material,
+                                const totri_array_t* scan_points,
+                                const totri_array_t* scan_origin,
+                                const totri_array_t* transient, float bin_width,
+                                float bin_offset, int model, void* workspace,
+                                size_t workspace_bytes, void* stream);
+
+/* Replaces totri_cpp.render.mesh_confocal_grad_verts
+ * (src/render/mesh.h:20-29, src/render/mesh.cpp:22-36).
+ * transient_grad [B,T,S]; verts_grad [B,V,3] or [B,V,0]; material_grad
+ * [B,V,M] or [B,V,0]; both gradients are overwritten. */
+int totri_mesh_confocal_grad_verts(const totri_array_t* verts, const totri_array_t* faces,
+                                   const totri_array_t* material,
+                                   const totri_array_t* scan_points,
+                                   const totri_array_t* scan_origin,
+                                   const totri_array_t* transient_grad,
+                                   const totri_array_t* verts_grad,
+                                   const totri_array_t* material_grad, float bin_width,
+                                   float bin_offset, int model, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
+/* Same as totri_mesh_confocal_grad_verts, but reuses the BVH and visibility
+ * masks left in `workspace` by a totri_mesh_confocal_forward call on the same
+ * inputs (the autograd path keeps that workspace between forward and
+ * backward). No reference counterpart: the reference rebuilds both
+ * (src/render/mesh_cuda.cu:78). */
+int totri_mesh_confocal_grad_verts_reuse(const totri_array_t* verts,
+                                         const totri_array_t* faces,
+                                         const totri_array_t* material,
+                                         const totri_array_t* scan_points,
+                                         const totri_array_t* scan_origin,
+                                         const totri_array_t* transient_grad,
+                                         const totri_array_t* verts_grad,
+                                         const totri_array_t* material_grad,
+                                         float bin_width, float bin_offset, int model,
+                                         void* workspace, size_t workspace_bytes,
+                                         void* stream);
+
+/* Replaces totri_cpp.render.mesh_exhaustive_forward
+ * (src/render/mesh.h:31-42, src/render/mesh.cpp:38-52).
+ * laser_points [B,L,3], laser_origin [B,L,3] or [B,0,3]; transient [B,T,S,L]. */
+int totri_mesh_exhaustive_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                  const totri_array_t* material,
+                                  const totri_array_t* scan_points,
+                                  const totri_array_t* laser_points,
+                                  const totri_array_t* scan_origin,
+                                  const totri_array_t* laser_origin,
+                                  const totri_array_t* transient, float bin_width,
+                                  float bin_offset, int model, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* Replaces totri_cpp.render.mesh_exhaustive_grad_verts
+ * (src/render/mesh.h:44-56, src/render/mesh.cpp:54-71). */
+int totri_mesh_exhaustive_grad_verts(const totri_array_t* verts, const totri_array_t* faces,
+                                     const totri_array_t* material,
+                                     const totri_array_t* scan_points,
+                                     const totri_array_t* laser_points,
+                                     const totri_array_t* scan_origin,
+                                     const totri_array_t* laser_origin,
+                                     const totri_array_t* transient_grad,
+                                     const totri_array_t* verts_grad,
+                                     const totri_array_t* material_grad, float bin_width,
+                                     float bin_offset, int model, void* workspace,
+                                     size_t workspace_bytes, void* stream);
+
+/* Exhaustive gradient reusing the BVH and masks of a forward call's
+ * workspace (no reference counterpart; see the confocal variant). */
+int totri_mesh_exhaustive_grad_verts_reuse(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* laser_points,
+    const totri_array_t* scan_origin, const totri_array_t* laser_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bin_width, float bin_offset, int model,
+    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Visibility masks only (testing and diagnostics; no reference counterpart).
+ * mask [B,P,ceil(F/32)] int32 words: bit f%32 of word f/32 is set when face f
+ * is the closest hit of the ray from point p to the centroid of f.
+ * brute_force != 0 tests every face instead of walking the BVH. */
+int totri_mesh_visibility(const totri_array_t* verts, const totri_array_t* faces,
+                          const totri_array_t* points, const totri_array_t* mask,
+                          int brute_force, void* workspace, size_t workspace_bytes,
+                          void* stream);
+
+/* Reads the device status word of a mesh workspace (synchronises `stream`).
+ * Returns TOTRI_OK when no kernel reported a problem, else TOTRI_ERR_DEVICE
+ * and *flags receives the bit set (1: a face index >= V ended a face list,
+ * 2: a BVH walk hit its iteration cap). */
+int totri_mesh_workspace_status(const void* workspace, size_t workspace_bytes,
+                                uint32_t* flags, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* render: volumes                                                          */
+
+/* Replaces totri_cpp.render.volume_confocal_forward
+ * (src/render/volume.h:10-16, src/render/volume.cpp:7-23).
+ * volume [X,Y,Z], measurement_points [3,N], transient [N,T] (overwritten);
+ * volume_origin/volume_size are 3-vectors. f32 or f64 (all the same). */
+int totri_volume_confocal_forward(const totri_array_t* volume,
+                                  const totri_array_t* measurement_points,
+                                  const totri_array_t* transient, const float volume_origin[3],
+                                  const float volume_size[3], float bin_width,
+                                  float bin_offset, void* stream);
+
+/* Replaces totri_cpp.render.volume_confocal_grad_volume
+ * (src/render/volume.h:18-24, src/render/volume.cpp:25-41): the transposed
+ * operator, transient [N,T] -> volume [X,Y,Z] (overwritten). */
+int totri_volume_confocal_grad_volume(const totri_array_t* volume,
+                                      const totri_array_t* measurement_points,
+                                      const totri_array_t* transient,
+                                      const float volume_origin[3],
+                                      const float volume_size[3], float bin_width,
+                                      float bin_offset, void* stream);
+
+/* The exact adjoint of totri_volume_confocal_forward (no reference
+ * counterpart: the reference transposed operator includes samples in the top
+ * slice that the forward drops, src/render/volume_cuda.cu:49 vs :127). */
+int totri_volume_confocal_adjoint(const totri_array_t* volume,
+                                  const totri_array_t* measurement_points,
+                                  const totri_array_t* transient,
+                                  const float volume_origin[3], const float volume_size[3],
+                                  float bin_width, float bin_offset, void* stream);
+
+/* Replaces totri_cpp.render.volume_confocal_grad_measurement_points
+ * (src/render/volume.h:26-32, src/render/volume.cpp:43-81).
+ * measurement_points_grad [3,N] (overwritten). */
+int totri_volume_confocal_grad_measurement_points(
+    const totri_array_t* measurement_points_grad, const totri_array_t* volume,
+    const totri_array_t* measurement_points, const totri_array_t* transient_grad,
+    const float volume_origin[3], const float volume_size[3], float bin_width,
+    float bin_offset, void* stream);
+
+/* Replaces totri_cpp.render.volume_render_exhaustive_forward
+ * (src/render/volume.h:34-43, src/render/volume.cpp:83-96).
+ * volume [B,D,H,W]; scan_points [B,3,S]; laser_points [B,3,L];
+ * scan_origin [B,3,S|0]; laser_origin [B,3,L|0]; transient [B,T,S,L]
+ * (overwritten). */
+int totri_volume_exhaustive_forward(const totri_array_t* volume,
+                                    const totri_array_t* scan_points,
+                                    const totri_array_t* laser_points,
+                                    const totri_array_t* scan_origin,
+                                    const totri_array_t* laser_origin,
+                                    const totri_array_t* transient,
+                                    const float volume_start[3], const float volume_end[3],
+                                    float bin_width, float bin_offset, void* stream);
+
+/* Replaces totri_cpp.render.volume_render_exhaustive_grad_volume
+ * (src/render/volume.h:45-54, src/render/volume.cpp:98-111), whose kernel
+ * body is empty in the reference (src/render/volume_cuda.cu:428-430). This is
+ * the true adjoint of totri_volume_exhaustive_forward, which is linear in the
+ * volume (skipping empty voxels there changes nothing). volume_grad
+ * [B,D,H,W] (overwritten). */
+int totri_volume_exhaustive_grad_volume(const totri_array_t* transient_grad,
+                                        const totri_array_t* scan_points,
+                                        const totri_array_t* laser_points,
+                                        const totri_array_t* scan_origin,
+                                        const totri_array_t* laser_origin,
+                                        const totri_array_t* volume_grad,
+                                        const float volume_start[3],
+                                        const float volume_end[3], float bin_width,
+                                        float bin_offset, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* reconstruct: backprojection                                              */
+
+/* Replaces totri_cpp.reconstruct.backprojection_confocal_velten_forward
+ * (src/reconstruct/backprojection.h:21-29, backprojection.cpp:22-34).
+ * transient [B,T,S]; scan_points [B,S,3]; scan_origin [B,S|0,3];
+ * volume [B,D,H,W] (overwritten). */
+int totri_backprojection_confocal_velten_forward(
+    const totri_array_t* transient, const totri_array_t* scan_points,
+    const totri_array_t* scan_origin, const totri_array_t* volume,
+    const float volume_start[3], const float volume_end[3], float bin_width,
+    float bin_offset, void* stream);
+
+/* The adjoint of the Velten confocal backprojection: volume [B,D,H,W] ->
+ * transient [B,T,S] (overwritten). No reference counterpart. */
+int totri_backprojection_confocal_velten_adjoint(
+    const totri_array_t* volume, const totri_array_t* scan_points,
+    const totri_array_t* scan_origin, const totri_array_t* transient,
+    const float volume_start[3], const float volume_end[3], float bin_width,
+    float bin_offset, void* stream);
+
+/* Replaces totri_cpp.reconstruct.backprojection_exhaustive_velten_forward
+ * (src/reconstruct/backprojection.h:31-39, backprojection.cpp:36-49).
+ * transient [B,T,S,L]; scan_points [B,S,3]; laser_points [B,L,3]. */
+int totri_backprojection_exhaustive_velten_forward(
+    const totri_array_t* transient, const totri_array_t* scan_points,
+    const totri_array_t* laser_points, const totri_array_t* scan_origin,
+    const totri_array_t* laser_origin, const totri_array_t* volume,
+    const float volume_start[3], const float volume_end[3], float bin_width,
+    float bin_offset, void* stream);
+
+/* Replaces totri_cpp.reconstruct.backprojection_exhaustive_arellano_forward
+ * (src/reconstruct/backprojection.h:10-19, backprojection.cpp:8-20).
+ * transient [B,T,S,L]; points [B,3,S] / [B,3,L]; volume [B,D,H,W]
+ * (accumulated into, as the reference does; callers pass zeros). */
+int totri_backprojection_exhaustive_arellano_forward(
+    const totri_array_t* transient, const totri_array_t* scan_points,
+    const totri_array_t* laser_points, const totri_array_t* scan_origin,
+    const totri_array_t* laser_origin, const totri_array_t* volume,
+    const float volume_start[3], const float volume_end[3], float bin_width,
+    float bin_offset, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* util: RBF to volume                                                      */
+
+/* Replaces totri_cpp.util.rbf2volume_gaussian_forward
+ * (src/util/rbf2volume.h:10-14, src/util/rbf2volume.cpp:7-15).
+ * rbf [B,N,4+A] (A<=8); volume [B,1+A,D,H,W] (overwritten). */
+int totri_rbf2volume_gaussian_forward(const totri_array_t* rbf, const totri_array_t* volume,
+                                      const float volume_start[3],
+                                      const float volume_end[3], void* stream);
+
+/* Replaces totri_cpp.util.rbf2volume_gaussian_grad
+ * (src/util/rbf2volume.h:16-22, src/util/rbf2volume.cpp:17-28).
+ * rbf_grad [B,N,4+A] is accumulated into (callers pass zeros, as the
+ * reference's Python layer does). */
+int totri_rbf2volume_gaussian_grad(const totri_array_t* rbf, const totri_array_t* volume,
+                                   const totri_array_t* volume_grad,
+                                   const totri_array_t* rbf_grad,
+                                   const float volume_start[3], const float volume_end[3],
+                                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TOTRI_GB300_H */

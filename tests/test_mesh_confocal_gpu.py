@@ -1,0 +1,180 @@
+"""Confocal mesh path on the GPU against the CPU oracle.
+
+Tolerances (from the path's contract): visibility masks and bin decisions are
+exact (masks compared bit for bit); transients within rel-L2 1e-5 of the FP64
+oracle; vertex/albedo gradients within rel-L2 1e-3 of the FP64 oracle (FP32
+gradient arithmetic has cancellation of order 1e-4, which the oracle's own
+FP32 mode shows as well).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from totri_gb300 import scenes
+from totri_gb300.render import MeshRenderConfocal
+from totri_gb300.totri_cpp import render as R
+
+from mesh_util import np_scene, rel_l2, unpack_mask
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = 1e-5
+GRAD_TOL = 1e-3
+
+
+def _dev(s):
+    return {k: (v.cuda() if torch.is_tensor(v) else v) for k, v in s.items()}
+
+
+def _oracle_forward(n, vis, bin_def, origin=None):
+    return oracle.mesh_confocal_forward(n["verts"], n["faces"], n["colors"], n["scan_points"],
+                                        origin, vis, bin_def.num, bin_def.width,
+                                        bin_def.offset, fp64=True)
+
+
+def test_visibility_matches_brute_force_small(cuda_lib):
+    s = scenes.confocal_small()
+    d, n = _dev(s), np_scene(s)
+    F = n["faces"].shape[0]
+    ref = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    bf = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
+    bvh = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"])
+    assert np.array_equal(unpack_mask(bf[0].cpu().numpy(), F), ref)
+    assert np.array_equal(unpack_mask(bvh[0].cpu().numpy(), F), ref)
+    assert 0.2 < ref.mean() < 0.6
+
+
+def test_forward_small_matches_oracle(cuda_lib):
+    s = scenes.confocal_small()
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    ref = _oracle_forward(n, vis, bd)
+    out = torch.full((1, bd.num, n["scan_points"].shape[0]), 7.0, device="cuda")
+    R.mesh_confocal_forward(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                            torch.empty_like(d["scan_points"][:, :0]), out, bd.width,
+                            bd.offset, 0)
+    got = out[0].double().cpu().numpy()
+    assert rel_l2(got, ref) < FWD_TOL
+    # bins where the oracle has no contribution stay exactly zero
+    assert np.all(got[ref == 0] == 0)
+
+
+def test_forward_with_origin_and_int64_faces(cuda_lib):
+    s = scenes.confocal_small(seed=5)
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    origin = torch.tensor([[0.3, -0.2, -1.0]])
+    so = origin[:, None, :].expand(1, n["scan_points"].shape[0], 3)
+    vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    ref = oracle.mesh_confocal_forward(n["verts"], n["faces"], n["colors"], n["scan_points"],
+                                       so[0].numpy(), vis, 1024, bd.width, bd.offset, fp64=True)
+    out = torch.empty((1, 1024, n["scan_points"].shape[0]), device="cuda")
+    R.mesh_confocal_forward(d["verts"], d["faces"].long(), d["colors"], d["scan_points"],
+                            so.cuda(), out, bd.width, bd.offset, 0)
+    assert rel_l2(out[0].double().cpu().numpy(), ref) < FWD_TOL
+
+
+def test_grad_small_matches_oracle(cuda_lib):
+    s = scenes.confocal_small(seed=3)
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    S = n["scan_points"].shape[0]
+    vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    tg = np.random.default_rng(0).standard_normal((bd.num, S)).astype(np.float32)
+    rv, rm = oracle.mesh_confocal_grad(n["verts"], n["faces"], n["colors"], n["scan_points"],
+                                       None, vis, bd.num, bd.width, bd.offset, tg, fp64=True)
+    vg = torch.full_like(d["verts"], 3.0)
+    mg = torch.full_like(d["colors"], 3.0)
+    R.mesh_confocal_grad_verts(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                               torch.empty_like(d["scan_points"][:, :0]),
+                               torch.from_numpy(tg)[None].cuda(), vg, mg, bd.width, bd.offset, 0)
+    assert rel_l2(vg[0].double().cpu().numpy(), rv) < GRAD_TOL
+    assert rel_l2(mg[0].double().cpu().numpy(), rm) < GRAD_TOL
+
+
+def test_autograd_reuse_matches_plain_calls(cuda_lib):
+    s = scenes.confocal_small(seed=4)
+    d = _dev(s)
+    bd = s["bin_def"]
+    verts = d["verts"].clone().requires_grad_(True)
+    colors = d["colors"].clone().requires_grad_(True)
+    tr = MeshRenderConfocal.apply(verts, d["faces"], d["scan_points"], bd, colors)
+    g = torch.randn_like(tr)
+    tr.backward(g)
+    out = torch.empty_like(tr)
+    R.mesh_confocal_forward(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                            torch.empty_like(d["scan_points"][:, :0]), out, bd.width, bd.offset, 0)
+    vg = torch.empty_like(d["verts"])
+    mg = torch.empty_like(d["colors"])
+    R.mesh_confocal_grad_verts(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                               torch.empty_like(d["scan_points"][:, :0]), g, vg, mg, bd.width,
+                               bd.offset, 0)
+    # shared-memory atomics add in a run-dependent order: equal up to FP32 rounding
+    assert rel_l2(tr.detach().cpu().numpy(), out.cpu().numpy()) < 1e-6
+    assert rel_l2(verts.grad.cpu().numpy(), vg.cpu().numpy()) < 1e-5
+    assert rel_l2(colors.grad.cpu().numpy(), mg.cpu().numpy()) < 1e-5
+
+
+def test_padded_and_empty_faces(cuda_lib):
+    s = scenes.confocal_small(seed=6)
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    faces = d["faces"].clone()
+    faces[0, 200, 1] = -1  # the list ends at face 200
+    faces[0, 250, 0] = -5
+    vis = oracle.mesh_visibility(n["verts"], faces[0].cpu().numpy(), n["scan_points"])
+    assert vis[:, 200:].sum() == 0
+    ref = oracle.mesh_confocal_forward(n["verts"], faces[0].cpu().numpy(), n["colors"],
+                                       n["scan_points"], None, vis, bd.num, bd.width,
+                                       bd.offset, fp64=True)
+    out = torch.empty((1, bd.num, n["scan_points"].shape[0]), device="cuda")
+    R.mesh_confocal_forward(d["verts"], faces, d["colors"], d["scan_points"],
+                            torch.empty_like(d["scan_points"][:, :0]), out, bd.width, bd.offset, 0)
+    assert rel_l2(out[0].double().cpu().numpy(), ref) < FWD_TOL
+    empty = torch.full_like(out, 5.0)
+    R.mesh_confocal_forward(d["verts"], faces[:, :0], d["colors"], d["scan_points"],
+                            torch.empty_like(d["scan_points"][:, :0]), empty, bd.width,
+                            bd.offset, 0)
+    assert float(empty.abs().max()) == 0.0
+
+
+def test_batch_of_two_meshes(cuda_lib):
+    a = scenes.confocal_small(seed=7)
+    b = scenes.confocal_small(seed=8)
+    bd = a["bin_def"]
+    verts = torch.cat([a["verts"], b["verts"]]).cuda()
+    colors = torch.cat([a["colors"], b["colors"]]).cuda()
+    sp = torch.cat([a["scan_points"], b["scan_points"]]).cuda()
+    tr = MeshRenderConfocal.apply(verts, a["faces"].cuda().expand(2, -1, -1), sp, bd, colors)
+    for i, s in enumerate((a, b)):
+        n = np_scene(s)
+        vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+        ref = _oracle_forward(n, vis, bd)
+        assert rel_l2(tr[i].double().cpu().numpy(), ref) < FWD_TOL
+
+
+def test_differentiable_workload_visibility_and_forward(cuda_lib):
+    """Full-size differentiable scene (20,480 faces x 4,096 scan points): BVH masks
+    equal the GPU brute-force masks everywhere and the oracle on a sample of pairs;
+    the forward matches the FP64 oracle evaluated on those masks."""
+    s = scenes.confocal_differentiable()
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    F = n["faces"].shape[0]
+    bvh = unpack_mask(R.mesh_visibility(d["verts"], d["faces"], d["scan_points"])[0]
+                      .cpu().numpy(), F)
+    bf = unpack_mask(R.mesh_visibility(d["verts"], d["faces"], d["scan_points"],
+                                       brute_force=True)[0].cpu().numpy(), F)
+    assert np.array_equal(bvh, bf)
+    g = np.random.default_rng(1)
+    pp = g.integers(0, n["scan_points"].shape[0], 3000)
+    pf = g.integers(0, F, 3000)
+    ref = oracle.mesh_visibility_pairs(n["verts"], n["faces"], n["scan_points"], pp, pf)
+    assert np.array_equal(bvh[pp, pf], ref)
+    out = torch.empty((1, bd.num, n["scan_points"].shape[0]), device="cuda")
+    R.mesh_confocal_forward(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                            torch.empty_like(d["scan_points"][:, :0]), out, bd.width, bd.offset, 0)
+    ref = _oracle_forward(n, bvh, bd)
+    assert rel_l2(out[0].double().cpu().numpy(), ref) < FWD_TOL

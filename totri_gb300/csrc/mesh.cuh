@@ -1,0 +1,263 @@
+// Mesh scene: per-batch-item face records, LBVH and visibility masks, plus
+// the FP32 ray-triangle test and BVH walk used for the visibility query.
+//
+// The reference answers visibility with an OptiX closest-hit trace from each
+// wall point to each face centroid (mesh_confocal_forward_optix.cu:42-65,
+// closest-hit/miss programs :132-139). Here the same query runs over a
+// linear BVH (Karras 2012 hierarchy over 30-bit Morton codes) built by
+// hand-written kernels, with an explicit ray-triangle test whose FP32
+// rounding is fixed so that the result equals a brute-force test over all
+// faces bit for bit.
+#pragma once
+
+#include "common.cuh"
+
+namespace totri {
+namespace mesh {
+
+// ---------------------------------------------------------------------------
+// Records (all 64 B, four float4, sorted by Morton code of the centroid).
+//
+// TriRec:   (v0.xyz, e1.x) (e1.yz, e2.xy) (e2.z, lo.xyz) (hi.xyz, face)
+//           e1 = v1 - v0, e2 = v2 - v0 (FP32, original vertex order);
+//           lo/hi = face AABB grown by delta: hit points must lie inside.
+// ShadeRec: (v0.xyz, albedo) (v1.xyz, vi0) (v2.xyz, vi1) (c.xyz, vi2)
+//           original vertices, FP32 centroid, vertex indices.
+// Node:     (lo0.xyz, hi0.x) (hi0.yz, lo1.xy) (lo1.z, hi1.xyz) (c0, c1, -, -)
+//           child >= 0: internal node, child < 0: leaf ~child.
+
+struct Meta {
+  int n;          // faces before the first invalid one
+  int term_neg;   // 1 when the terminating face holds a negative index
+  float scale;    // max |coordinate| over referenced vertices
+  float delta;    // scale * 2^-12: hit-point box margin
+  int cmin[3];    // ford()-encoded centroid bounds (Morton frame)
+  int cmax[3];
+  int pad[6];
+};
+
+struct Scene {
+  int B;           // batch items
+  int F;           // face capacity per item
+  int nch;         // ceil(F / 32) mask words per point
+  int P;           // points per item (mask rows)
+  Meta* meta;      // [B]
+  uint32_t* keys;  // [B][2][F] ping-pong sort buffers
+  uint32_t* vals;  // [B][2][F]
+  float4* tri;     // [B][F][4]
+  float4* shade;   // [B][F][4]
+  float4* nodes;   // [B][F][4] (F-1 used)
+  int* lparent;    // [B][F]
+  int* iparent;    // [B][F]
+  int* counter;    // [B][F]
+  uint32_t* mask;  // [B][P][nch]
+  uint32_t* status;
+  int sorted_buf;  // which ping-pong half holds the sorted keys (0/1)
+};
+
+// Mesh inputs of one call.
+struct BuildInputs {
+  View3f verts;      // [B, V, 3]
+  View3i faces;      // [B, F, 3]
+  View3f material;   // [B, V, M]
+  int M;
+  int64_t V;
+  int F;             // input faces per item
+};
+
+// Workspace layout on the host.
+struct Layout {
+  size_t header, meta, keys, vals, tri, shade, nodes, lparent, iparent, counter, mask, total;
+};
+
+inline Layout layout(int64_t B, int64_t F, int64_t P) {
+  Layout L{};
+  const int64_t Fc = F > 0 ? F : 1;
+  const int64_t nch = (Fc + 31) / 32;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  L.header = take(256);
+  L.meta = take(sizeof(Meta) * B);
+  L.keys = take(sizeof(uint32_t) * 2 * B * Fc);
+  L.vals = take(sizeof(uint32_t) * 2 * B * Fc);
+  L.tri = take(64 * B * Fc);
+  L.shade = take(64 * B * Fc);
+  L.nodes = take(64 * B * Fc);
+  L.lparent = take(sizeof(int) * B * Fc);
+  L.iparent = take(sizeof(int) * B * Fc);
+  L.counter = take(sizeof(int) * B * Fc);
+  L.mask = take(sizeof(uint32_t) * B * P * nch);
+  L.total = off;
+  return L;
+}
+
+inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
+  const Layout L = layout(B, F, P);
+  char* base = static_cast<char*>(ws);
+  Scene s;
+  s.B = (int)B;
+  s.F = (int)(F > 0 ? F : 1);
+  s.nch = (int)((s.F + 31) / 32);
+  s.P = (int)P;
+  s.status = reinterpret_cast<uint32_t*>(base + L.header);
+  s.meta = reinterpret_cast<Meta*>(base + L.meta);
+  s.keys = reinterpret_cast<uint32_t*>(base + L.keys);
+  s.vals = reinterpret_cast<uint32_t*>(base + L.vals);
+  s.tri = reinterpret_cast<float4*>(base + L.tri);
+  s.shade = reinterpret_cast<float4*>(base + L.shade);
+  s.nodes = reinterpret_cast<float4*>(base + L.nodes);
+  s.lparent = reinterpret_cast<int*>(base + L.lparent);
+  s.iparent = reinterpret_cast<int*>(base + L.iparent);
+  s.counter = reinterpret_cast<int*>(base + L.counter);
+  s.mask = reinterpret_cast<uint32_t*>(base + L.mask);
+  s.sorted_buf = 1;  // three 10-bit radix passes end in the second half
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Device helpers.
+
+__device__ __forceinline__ const float4* tri_at(const Scene& s, int b, int k) {
+  return s.tri + ((size_t)b * s.F + k) * 4;
+}
+__device__ __forceinline__ const float4* shade_at(const Scene& s, int b, int k) {
+  return s.shade + ((size_t)b * s.F + k) * 4;
+}
+__device__ __forceinline__ const float4* node_at(const Scene& s, int b, int i) {
+  return s.nodes + ((size_t)b * s.F + i) * 4;
+}
+
+// FP32 ray-triangle test (two-sided Moller-Trumbore with t in [0, tmax] and
+// the hit point fma(t, d, o) inside the grown face AABB). Mirrors
+// oracle/mesh.cpp tri_hit operation for operation.
+__device__ __forceinline__ bool tri_hit(float4 t0, float4 t1, float4 t2, float4 t3, fv3 o,
+                                        fv3 d, float tmax, float& tout) {
+  const fv3 v0 = mkv(t0.x, t0.y, t0.z);
+  const fv3 e1 = mkv(t0.w, t1.x, t1.y);
+  const fv3 e2 = mkv(t1.z, t1.w, t2.x);
+  const fv3 p = xcross(d, e2);
+  const float det = xdot(e1, p);
+  if (det == 0.f) return false;
+  const float inv = xrcp(det);
+  const fv3 tv = xsub3(o, v0);
+  const float u = xmul(xdot(tv, p), inv);
+  if (!(u >= 0.f && u <= 1.f)) return false;
+  const fv3 q = xcross(tv, e1);
+  const float v = xmul(xdot(d, q), inv);
+  if (!(v >= 0.f && xadd(u, v) <= 1.f)) return false;
+  const float t = xmul(xdot(e2, q), inv);
+  if (!(t >= 0.f && t <= tmax)) return false;
+  const float px = xfma(t, d.x, o.x);
+  const float py = xfma(t, d.y, o.y);
+  const float pz = xfma(t, d.z, o.z);
+  if (!(px >= t2.y && px <= t3.x && py >= t2.z && py <= t3.y && pz >= t2.w && pz <= t3.z))
+    return false;
+  tout = t;
+  return true;
+}
+
+// Slab test of a BVH box against the ray segment [0, limit]. Boxes carry a
+// margin of at least delta beyond every accepted hit point, which dominates
+// the rounding of this test, so a box holding a hit is never rejected.
+__device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy,
+                                     float hz, fv3 inv, fv3 oinv, float limit,
+                                     float& tnear) {
+  const float tx0 = fmaf(lx, inv.x, -oinv.x), tx1 = fmaf(hx, inv.x, -oinv.x);
+  const float ty0 = fmaf(ly, inv.y, -oinv.y), ty1 = fmaf(hy, inv.y, -oinv.y);
+  const float tz0 = fmaf(lz, inv.z, -oinv.z), tz1 = fmaf(hz, inv.z, -oinv.z);
+  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
+  const float tf =
+      fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), limit));
+  tnear = tn;
+  return tn <= tf;
+}
+
+__device__ __forceinline__ float safe_inv(float d) {
+  return fabsf(d) < 1e-20f ? copysignf(1e20f, d) : 1.f / d;
+}
+
+// True when face k (sorted position) is the closest hit, lowest face index on
+// ties, of the ray from o to its centroid within [0, 1.01 d + 1e-3]
+// (mesh_confocal_forward_optix.cu:42-65). brute: test every face instead of
+// walking the BVH (same answer by construction).
+template <bool kBrute>
+__device__ bool face_visible(const Scene& sc, int b, int n, int k, fv3 o, uint32_t* status) {
+  const float4* sr = shade_at(sc, b, k);
+  const float4 c4 = __ldg(sr + 3);
+  const fv3 c = mkv(c4.x, c4.y, c4.z);
+  const fv3 D = xsub3(c, o);
+  const float dist = xlen(D);
+  if (!(dist >= 1e-6f)) return false;
+  const fv3 dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+  const float tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+  const float4* tr = tri_at(sc, b, k);
+  const float4 a0 = __ldg(tr), a1 = __ldg(tr + 1), a2 = __ldg(tr + 2), a3 = __ldg(tr + 3);
+  const int f = __float_as_int(a3.w);
+  float tf;
+  if (!tri_hit(a0, a1, a2, a3, o, dir, tmax, tf)) return false;
+
+  auto occludes = [&](int kk) -> bool {
+    if (kk == k) return false;
+    if (kk < 0 || kk >= n) {
+      atomicOr(status, kStatusTraversalCap);
+      return false;
+    }
+    const float4* q = tri_at(sc, b, kk);
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+    float tg;
+    if (!tri_hit(q0, q1, q2, q3, o, dir, tmax, tg)) return false;
+    return tg < tf || (tg == tf && __float_as_int(q3.w) < f);
+  };
+
+  if (kBrute || n == 1) {
+    for (int kk = 0; kk < n; ++kk)
+      if (occludes(kk)) return false;
+    return true;
+  }
+
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  int stack[64];
+  int sp = 0;
+  int node = 0;
+  const int cap = 2 * n + 64;
+  for (int it = 0; it < cap; ++it) {
+    if (node < 0 || node >= n - 1) break;  // malformed tree: flagged below
+    const float4* nd = node_at(sc, b, node);
+    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+    float tn0, tn1;
+    bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
+    bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    if (h0 && c0 < 0) {
+      if (occludes(~c0)) return false;
+      h0 = false;
+    }
+    if (h1 && c1 < 0) {
+      if (occludes(~c1)) return false;
+      h1 = false;
+    }
+    if (h0 && h1) {
+      const bool first0 = tn0 <= tn1;
+      if (sp < 64) stack[sp++] = first0 ? c1 : c0;
+      else atomicOr(status, kStatusTraversalCap);
+      node = first0 ? c0 : c1;
+    } else if (h0) {
+      node = c0;
+    } else if (h1) {
+      node = c1;
+    } else {
+      if (sp == 0) return true;
+      node = stack[--sp];
+    }
+  }
+  atomicOr(status, kStatusTraversalCap);
+  return true;
+}
+
+}  // namespace mesh
+}  // namespace totri

@@ -1,0 +1,301 @@
+// Confocal mesh transient rendering: visibility masks, forward splat and the
+// vertex / albedo gradient.
+//
+// Reference: src/render/program/mesh_confocal_forward_optix.cu:18-129 and
+// mesh_confocal_grad_verts_optix.cu:18-190 (one OptiX thread per
+// (face, scan point) with global atomics into transient[b][bin][s] and into
+// verts_grad). Here:
+//  * visibility runs once per (scan point, face) into a bit mask
+//    [B][P][ceil(F/32)] (one warp per 32 Morton-ordered faces of a point);
+//  * the forward gives each CTA a tile of TS scan points and walks all faces,
+//    splatting into a shared-memory histogram [T][TS] with shared atomics, and
+//    flushes the tile with coalesced float4 stores (no global atomics, no
+//    separate zero fill);
+//  * the gradient gives each CTA one 32-face mask word and walks all scan
+//    points (lanes over s, so transient_grad reads are row-coalesced), keeps
+//    the per-face gradient in registers, reduces it across the warp and issues
+//    12 atomics per face instead of 9 + 3M per visible pair.
+#include "mesh.cuh"
+#include "mesh_kernels.cuh"
+
+namespace totri {
+namespace mesh {
+
+namespace {
+
+template <bool kBrute>
+__global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t per_b = (int64_t)P * sc.nch;
+  if (gw >= per_b * sc.B) return;
+  const int b = (int)(gw / per_b);
+  const int64_t rem = gw - (int64_t)b * per_b;
+  const int p = (int)(rem / sc.nch);
+  const int ch = (int)(rem - (int64_t)p * sc.nch);
+  const int n = sc.meta[b].n;
+  const int k = ch * 32 + lane;
+  bool vis = false;
+  if (k < n) {
+    const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
+    vis = face_visible<kBrute>(sc, b, n, k, o, sc.status);
+  }
+  const uint32_t word = __ballot_sync(0xffffffffu, vis);
+  if (lane == 0) sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
+}
+
+// Per-pair confocal geometry: FP32 decisions exactly as the oracle takes them.
+struct ConfocalPair {
+  fv3 v[3];
+  int perm[3];
+  float d[3];
+  float c[3];
+  int bin[3];
+};
+
+__device__ __forceinline__ void confocal_pair(const float4 s0, const float4 s1, const float4 s2,
+                                              fv3 sp, float od, float bw, float bo,
+                                              ConfocalPair& q) {
+  q.v[0] = mkv(s0.x, s0.y, s0.z);
+  q.v[1] = mkv(s1.x, s1.y, s1.z);
+  q.v[2] = mkv(s2.x, s2.y, s2.z);
+  for (int k = 0; k < 3; ++k) {
+    q.perm[k] = k;
+    q.d[k] = xlen(xsub3(q.v[k], sp));
+  }
+  sort3(q);
+  for (int k = 0; k < 3; ++k) {
+    q.c[k] = xdiv(xsub(xadd(xmul(2.f, q.d[k]), od), bo), bw);
+    q.bin[k] = bin_of(q.c[k]);
+  }
+}
+
+// alpha of AlphaConfocal (mesh_common.h:394-413):
+// 100 rho (n_w.r)^2 (n.r)^2 / (|n| |r|^8), n_w = (0,0,1), r = c - s.
+__device__ __forceinline__ float alpha_confocal(const ConfocalPair& q, fv3 c, fv3 sp,
+                                                float rho) {
+  const fv3 n = cross(q.v[1] - q.v[0], q.v[2] - q.v[0]);
+  const fv3 r = c - sp;
+  if (!(r.z > 0.f)) return 0.f;
+  const float nr = dot(n, r), rr = dot(r, r), nn = dot(n, n);
+  const float rr2 = rr * rr;
+  return 100.f * rho * (r.z * r.z) * (nr * nr) / (sqrtf(nn) * (rr2 * rr2));
+}
+
+template <int TS>
+__global__ void __launch_bounds__(256) splat_kernel(Scene sc, View3f sp, View3f so, int has_origin,
+                                                    float* __restrict__ transient, int T, int S,
+                                                    float bw, float bo) {
+  extern __shared__ float hist[];  // [T][TS]
+  const int b = blockIdx.y;
+  const int s0 = blockIdx.x * TS;
+  for (int i = threadIdx.x; i < T * TS; i += blockDim.x) hist[i] = 0.f;
+  __syncthreads();
+  const int n = sc.meta[b].n;
+  const int sl = threadIdx.x % TS;
+  const int s = s0 + sl;
+  if (s < S) {
+    const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+    float od = 0.f;
+    if (has_origin) od = xmul(2.f, xlen(xsub3(p, mkv(so.at(b, s, 0), so.at(b, s, 1), so.at(b, s, 2)))));
+    const uint32_t* mrow = sc.mask + ((size_t)b * sc.P + s) * sc.nch;
+    const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+    Hist<TS> h{hist, sl, T};
+    for (int k = threadIdx.x / TS; k < n; k += blockDim.x / TS) {
+      if (!((__ldg(mrow + (k >> 5)) >> (k & 31)) & 1u)) continue;
+      const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+      const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+      ConfocalPair q;
+      confocal_pair(s0r, s1r, s2r, p, od, bw, bo, q);
+      const float alpha = alpha_confocal(q, mkv(s3r.x, s3r.y, s3r.z), p, s0r.w);
+      if (!(alpha > 0.f)) continue;
+      splat_tent(h, q.c, q.bin, alpha);
+    }
+  }
+  __syncthreads();
+  flush_tile<TS>(hist, transient + (size_t)b * T * S, T, S, s0);
+}
+
+// Gradient of one visible pair with respect to the three (sorted) vertices and
+// the albedo, following mesh_confocal_grad_verts_optix.cu:248-314 and
+// AlphaConfocalGradVerts (mesh_common.h:429-463). Returns false when the pair
+// contributes nothing.
+__device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c, fv3 p, float rho,
+                                                   float bw, const float* __restrict__ tg_col,
+                                                   int T, int S, fv3 dv[3], float& dmat) {
+  const float alpha = alpha_confocal(q, c, p, rho);
+  if (!(alpha > 0.f)) return false;
+  if (q.bin[0] >= T || q.bin[2] < 0) return false;
+  const fv3 e1 = q.v[1] - q.v[0], e2 = q.v[2] - q.v[0];
+  const fv3 n = cross(e1, e2);
+  const fv3 r = c - p;
+  // d log(alpha) / d v_k = J_n^T (kn n + knr r) + kr r + (knr/3) n + kw n_w
+  const float kn = -1.f / dot(n, n);
+  const float kr = -8.f / (3.f * dot(r, r));
+  const float kw = 2.f / (3.f * r.z);
+  const float knr = 2.f / dot(n, r);
+  const fv3 w = kn * n + knr * r;
+  const fv3 g1 = cross(e2, w), g2 = cross(w, e1);
+  const fv3 common = kr * r + (knr * (1.f / 3.f)) * n + mkv(0.f, 0.f, kw);
+  const fv3 da0 = alpha * (common - g1 - g2);
+  const fv3 da1 = alpha * (common + g1);
+  const fv3 da2 = alpha * (common + g2);
+  const float dadm = alpha / rho;
+  if (q.bin[0] == q.bin[2]) {
+    const float g = __ldg(tg_col + (size_t)q.bin[0] * S);
+    dv[0] = g * da0;
+    dv[1] = g * da1;
+    dv[2] = g * da2;
+    dmat = g * dadm;
+    return true;
+  }
+  TentGrad tgr;
+  tent_grad(tg_col, S, T, q.c, q.bin, tgr);
+  // part1 = Ayc * dyc + A0 * dc0 + A1 * dc1 + A2 * dc2 (see TentGrad)
+  const float span = q.c[2] - q.c[0];
+  const float kk = -4.f / (bw * span * span);
+  const fv3 r0 = q.v[0] - p, r1 = q.v[1] - p, r2 = q.v[2] - p;
+  const fv3 dc0 = (2.f / (bw * q.d[0])) * r0;
+  const fv3 dc1 = (2.f / (bw * q.d[1])) * r1;
+  const fv3 dc2 = (2.f / (bw * q.d[2])) * r2;
+  const fv3 dyc0 = (kk / -q.d[0]) * r0;
+  const fv3 dyc2 = (kk / q.d[2]) * r2;
+  const fv3 p1_0 = tgr.ayc * dyc0 + tgr.a0 * dc0;
+  const fv3 p1_1 = tgr.a1 * dc1;
+  const fv3 p1_2 = tgr.ayc * dyc2 + tgr.a2 * dc2;
+  dv[0] = tgr.part0 * da0 + alpha * p1_0;
+  dv[1] = tgr.part0 * da1 + alpha * p1_1;
+  dv[2] = tgr.part0 * da2 + alpha * p1_2;
+  dmat = dadm * tgr.part0;
+  return true;
+}
+
+__global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f so, int has_origin,
+                                                   const float* __restrict__ tgrad, int T, int S,
+                                                   float bw, float bo, GradOut out) {
+  extern __shared__ uint32_t mcol[];  // [S] mask words of this 32-face chunk
+  const int b = blockIdx.y;
+  const int ch = blockIdx.x;
+  const int n = sc.meta[b].n;
+  if (ch * 32 >= n) return;
+  for (int s = threadIdx.x; s < S; s += blockDim.x)
+    mcol[s] = sc.mask[((size_t)b * sc.P + s) * sc.nch + ch];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const float* tgb = tgrad + (size_t)b * T * S;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  for (int j = warp; j < 32; j += nw) {
+    const int k = ch * 32 + j;
+    if (k >= n) break;
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
+    fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
+    float accm = 0.f;
+    for (int s = lane; s < S; s += 32) {
+      if (!((mcol[s] >> j) & 1u)) continue;
+      const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+      float od = 0.f;
+      if (has_origin)
+        od = xmul(2.f, xlen(xsub3(p, mkv(so.at(b, s, 0), so.at(b, s, 1), so.at(b, s, 2)))));
+      ConfocalPair q;
+      confocal_pair(s0r, s1r, s2r, p, od, bw, bo, q);
+      fv3 dv[3];
+      float dm;
+      if (!pair_grad_confocal(q, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) continue;
+      for (int kk = 0; kk < 3; ++kk) acc[q.perm[kk]] = acc[q.perm[kk]] + dv[kk];
+      accm += dm;
+    }
+    scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
+  }
+}
+
+// Re-indexes mask bits from Morton order (bit k) to input face order (bit f).
+__global__ void mask_unsort_kernel(Scene sc, int P, uint32_t* out) {
+  const int b = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = sc.meta[b].n;
+  if (i >= (int64_t)P * n) return;
+  const int p = (int)(i / n), k = (int)(i - (int64_t)p * n);
+  const uint32_t w = sc.mask[((size_t)b * sc.P + p) * sc.nch + (k >> 5)];
+  if (!((w >> (k & 31)) & 1u)) return;
+  const int f = __float_as_int(tri_at(sc, b, k)[3].w);
+  atomicOr(out + ((size_t)b * P + p) * sc.nch + (f >> 5), 1u << (f & 31));
+}
+
+}  // namespace
+
+int launch_mask_unsort(const Scene& sc, int P, uint32_t* out, cudaStream_t stream) {
+  TOTRI_CUDA(cudaMemsetAsync(out, 0, sizeof(uint32_t) * (size_t)sc.B * P * sc.nch, stream));
+  const dim3 grid((unsigned)ceil_div((int64_t)P * sc.F, 256), (unsigned)sc.B);
+  TOTRI_KERNEL("mesh mask unsort", stream, mask_unsort_kernel<<<grid, 256, 0, stream>>>(sc, P, out));
+  return TOTRI_OK;
+}
+
+int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool brute,
+                      cudaStream_t stream) {
+  const int64_t warps = (int64_t)sc.B * P * sc.nch;
+  if (warps == 0) return TOTRI_OK;
+  const int64_t blocks = ceil_div(warps * 32, 256);
+  if (brute)
+    TOTRI_KERNEL("mesh visibility brute", stream,
+                 visibility_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(sc, pts, P, row0));
+  else
+    TOTRI_KERNEL("mesh visibility", stream,
+                 visibility_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(sc, pts, P, row0));
+  return TOTRI_OK;
+}
+
+template <int TS>
+static int launch_splat_ts(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
+                           float* transient, int T, int S, float bw, float bo,
+                           cudaStream_t stream) {
+  const size_t smem = sizeof(float) * (size_t)T * TS;
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(splat_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    configured = (int)smem;
+  }
+  const dim3 grid((unsigned)ceil_div(S, TS), (unsigned)sc.B);
+  TOTRI_KERNEL("mesh confocal splat", stream,
+               splat_kernel<TS><<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, transient, T,
+                                                             S, bw, bo));
+  return TOTRI_OK;
+}
+
+int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
+                          float* transient, int T, int S, float bw, float bo,
+                          cudaStream_t stream) {
+  const size_t budget = 200 * 1024;
+  if ((size_t)T * 8 * 4 <= budget && S >= 8 * 152)
+    return launch_splat_ts<8>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+  if ((size_t)T * 4 * 4 <= budget && S >= 4 * 152)
+    return launch_splat_ts<4>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+  if ((size_t)T * 2 * 4 <= budget && S >= 2 * 152)
+    return launch_splat_ts<2>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+  if ((size_t)T * 4 <= budget)
+    return launch_splat_ts<1>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+  return fail(TOTRI_ERR_UNSUPPORTED, "number of bins too large for the shared-memory tile");
+}
+
+int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
+                         const float* tgrad, int T, int S, float bw, float bo,
+                         const GradOut& out, cudaStream_t stream) {
+  const size_t smem = sizeof(uint32_t) * (size_t)S;
+  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many scan points for one tile");
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    configured = (int)smem;
+  }
+  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B);
+  TOTRI_KERNEL("mesh confocal grad", stream,
+               grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, tgrad, T, S, bw,
+                                                        bo, out));
+  return TOTRI_OK;
+}
+
+}  // namespace mesh
+}  // namespace totri

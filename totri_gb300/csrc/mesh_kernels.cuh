@@ -1,0 +1,230 @@
+// Device building blocks shared by the confocal and exhaustive mesh kernels:
+// the vertex sort, the tent splat into a shared-memory tile, the tile flush,
+// the tent gradient and the per-face gradient scatter.
+#pragma once
+
+#include "mesh.cuh"
+
+namespace totri {
+namespace mesh {
+
+// Sorts the three vertices by FP32 path length with the reference's
+// compare-swap sequence (mesh_confocal_forward_optix.cu:86-101). Ties keep the
+// original order.
+template <class Q>
+__device__ __forceinline__ void sort3(Q& q) {
+  auto sw = [&](int i, int j) {
+    float td = q.d[i]; q.d[i] = q.d[j]; q.d[j] = td;
+    fv3 tv = q.v[i]; q.v[i] = q.v[j]; q.v[j] = tv;
+    int tp = q.perm[i]; q.perm[i] = q.perm[j]; q.perm[j] = tp;
+  };
+  if (q.d[0] > q.d[1]) sw(0, 1);
+  if (q.d[1] > q.d[2]) sw(1, 2);
+  if (q.d[0] > q.d[1]) sw(0, 1);
+}
+
+// One wall column of a shared-memory histogram [T][TS].
+template <int TS>
+struct Hist {
+  float* h;
+  int sl;
+  int T;
+  __device__ __forceinline__ bool in(int b) const { return b >= 0 && b < T; }
+  __device__ __forceinline__ void add(int b, float v) const { atomicAdd(h + b * TS + sl, v); }
+};
+
+// DrawTrapezoid (mesh_common.h:61-94): integrates the line through
+// (ca, ya) - (cb, yb) over each bin it spans (midpoint rule, exact for a line).
+template <class H>
+__device__ __forceinline__ void splat_segment(const H& h, float ca, int ba, float ya, float cb,
+                                              int bb, float yb) {
+  if (ba == bb) {
+    if (h.in(ba)) h.add(ba, 0.5f * (cb - ca) * (ya + yb));
+    return;
+  }
+  const float slope = (yb - ya) / (cb - ca);
+  if (h.in(ba)) {
+    const float w = (float)(ba + 1) - ca;
+    h.add(ba, w * (ya + 0.5f * w * slope));
+  }
+  const int lo = max(ba + 1, 0), hi = min(bb, h.T);
+  for (int i = lo; i < hi; ++i) h.add(i, ya + (((float)i + 0.5f) - ca) * slope);
+  if (h.in(bb)) {
+    const float w = cb - (float)bb;
+    h.add(bb, w * (ya + (0.5f * ((float)bb + cb) - ca) * slope));
+  }
+}
+
+// The triangle's time profile: a tent of area alpha from c0 to c2 peaking at
+// c1 (mesh_confocal_forward_optix.cu:114-129).
+template <class H>
+__device__ __forceinline__ void splat_tent(const H& h, const float c[3], const int bin[3],
+                                           float alpha) {
+  if (bin[0] >= h.T || bin[2] < 0) return;
+  if (bin[0] == bin[2]) {
+    h.add(bin[0], alpha);
+    return;
+  }
+  const float yc = 2.f * alpha / (c[2] - c[0]);
+  splat_segment(h, c[0], bin[0], 0.f, c[1], bin[1], yc);
+  splat_segment(h, c[1], bin[1], yc, c[2], bin[2], 0.f);
+}
+
+// Writes a [T][TS] shared tile to out[t * S + s0 + j] (coalesced; float4 when
+// the rows are 16-byte aligned).
+template <int TS>
+__device__ __forceinline__ void flush_tile(const float* hist, float* __restrict__ out, int T,
+                                           int S, int s0) {
+  const bool vec = (TS % 4 == 0) && (S % 4 == 0) && (s0 + TS <= S) &&
+                   ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+  if (vec) {
+    constexpr int Q = TS / 4 > 0 ? TS / 4 : 1;
+    const float4* h4 = reinterpret_cast<const float4*>(hist);
+    for (int idx = threadIdx.x; idx < T * Q; idx += blockDim.x) {
+      const int row = idx / Q, q = idx - row * Q;
+      *reinterpret_cast<float4*>(out + (size_t)row * S + s0 + 4 * q) = h4[idx];
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < T * TS; idx += blockDim.x) {
+      const int row = idx / TS, j = idx - row * TS;
+      if (s0 + j < S) out[(size_t)row * S + s0 + j] = hist[idx];
+    }
+  }
+}
+
+// Gradient of the normalised tent (area 1, yc = 2 / (c2 - c0)) against the
+// incoming transient gradient g(bin) = col[bin * stride]:
+//   part0 = sum_bins g * area_bin
+//   part1 = ayc * d(yc) + a0 * d(c0) + a1 * d(c1) + a2 * d(c2)
+// which is DrawTrapezoidGrad (mesh_common.h:104-199) for both segments with the
+// vector terms factored out of the bin sum.
+struct TentGrad {
+  float part0, ayc, a0, a1, a2;
+};
+
+struct SegSums {
+  float ya, yb, ca, cb;
+};
+
+__device__ __forceinline__ void grad_segment(const float* __restrict__ col, int64_t stride, int T,
+                                             float& part0, SegSums& sm, float ca, int ba, float ya,
+                                             float cb, int bb, float yb) {
+  auto in = [&](int b) { return b >= 0 && b < T; };
+  if (ba == bb) {
+    if (in(ba)) {
+      const float g = __ldg(col + ba * stride);
+      const float half_span = 0.5f * (cb - ca), half_y = 0.5f * (ya + yb);
+      part0 += g * half_span * (ya + yb);
+      sm.ya += g * half_span;
+      sm.yb += g * half_span;
+      sm.ca -= g * half_y;
+      sm.cb += g * half_y;
+    }
+    return;
+  }
+  const float inv = 1.f / (cb - ca);
+  const float slope = (yb - ya) * inv;
+  const float q = slope * inv;
+  if (in(ba)) {
+    const float g = __ldg(col + ba * stride);
+    const float base = (float)(ba + 1) - ca;
+    const float hb2 = 0.5f * base * base;
+    part0 += g * base * (ya + 0.5f * base * slope);
+    sm.ya += g * (base - hb2 * inv);
+    sm.yb += g * hb2 * inv;
+    sm.ca += g * (-ya - base * slope + hb2 * q);
+    sm.cb -= g * hb2 * q;
+  }
+  float sg = 0.f, sgm = 0.f;
+  const int lo = max(ba + 1, 0), hi = min(bb, T);
+  for (int i = lo; i < hi; ++i) {
+    const float g = __ldg(col + i * stride);
+    sg += g;
+    sgm += g * (((float)i + 0.5f) - ca);
+  }
+  part0 += ya * sg + slope * sgm;
+  sm.ya += sg - inv * sgm;
+  sm.yb += inv * sgm;
+  sm.ca += -slope * sg + q * sgm;
+  sm.cb -= q * sgm;
+  if (in(bb)) {
+    const float g = __ldg(col + bb * stride);
+    const float w = cb - (float)bb;
+    const float mid = 0.5f * ((float)bb + cb) - ca;
+    part0 += g * w * (ya + mid * slope);
+    sm.ya += g * w * (1.f - mid * inv);
+    sm.yb += g * w * mid * inv;
+    sm.ca += g * w * (-slope + mid * q);
+    sm.cb += g * ((ya + mid * slope) + w * (0.5f * slope - mid * q));
+  }
+}
+
+__device__ __forceinline__ void tent_grad(const float* __restrict__ col, int64_t stride, int T,
+                                          const float c[3], const int bin[3], TentGrad& out) {
+  const float yc = 2.f / (c[2] - c[0]);
+  float part0 = 0.f;
+  SegSums s1{0.f, 0.f, 0.f, 0.f}, s2{0.f, 0.f, 0.f, 0.f};
+  grad_segment(col, stride, T, part0, s1, c[0], bin[0], 0.f, c[1], bin[1], yc);
+  grad_segment(col, stride, T, part0, s2, c[1], bin[1], yc, c[2], bin[2], 0.f);
+  out.part0 = part0;
+  out.ayc = s1.yb + s2.ya;
+  out.a0 = s1.ca;
+  out.a1 = s1.cb + s2.ca;
+  out.a2 = s2.cb;
+}
+
+// Gradient outputs (strided, may be absent).
+struct GradOut {
+  float* vg;           // [B, V, 3] or null
+  int64_t vsb, vsv, vsc;
+  float* mg;           // [B, V, Mg] (channel 0 receives the albedo gradient) or null
+  int64_t msb, msv, msc;
+  int64_t V;
+};
+
+__device__ __forceinline__ float warp_sum(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Reduces one face's gradient over the warp and adds it to its vertices
+// (mesh_confocal_grad_verts_optix.cu:316-332; 1/3 of the albedo gradient
+// goes to channel 0 of each vertex).
+__device__ __forceinline__ void scatter_face_grad(const GradOut& out, int b, float4 s1r, float4 s2r,
+                                                  float4 s3r, fv3 acc[3], float accm,
+                                                  uint32_t* status) {
+  float v[10] = {acc[0].x, acc[0].y, acc[0].z, acc[1].x, acc[1].y,
+                 acc[1].z, acc[2].x, acc[2].y, acc[2].z, accm};
+#pragma unroll
+  for (int i = 0; i < 10; ++i) v[i] = warp_sum(v[i]);
+  if ((threadIdx.x & 31) != 0) return;
+  const int vi[3] = {__float_as_int(s1r.w), __float_as_int(s2r.w), __float_as_int(s3r.w)};
+  for (int q = 0; q < 3; ++q) {
+    if (vi[q] < 0 || vi[q] >= out.V) {
+      atomicOr(status, kStatusFaceIndexRange);
+      continue;
+    }
+    if (out.vg) {
+      float* p = out.vg + b * out.vsb + vi[q] * out.vsv;
+      atomicAdd(p, v[3 * q]);
+      atomicAdd(p + out.vsc, v[3 * q + 1]);
+      atomicAdd(p + 2 * out.vsc, v[3 * q + 2]);
+    }
+    if (out.mg) atomicAdd(out.mg + b * out.msb + vi[q] * out.msv, (1.f / 3.f) * v[9]);
+  }
+}
+
+// Host launchers.
+int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool brute,
+                      cudaStream_t stream);
+int launch_mask_unsort(const Scene& sc, int P, uint32_t* out, cudaStream_t stream);
+int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
+                          float* transient, int T, int S, float bw, float bo, cudaStream_t stream);
+int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
+                         const float* tgrad, int T, int S, float bw, float bo, const GradOut& out,
+                         cudaStream_t stream);
+
+int build_scene(const Scene& sc, const BuildInputs& in, cudaStream_t stream);
+
+}  // namespace mesh
+}  // namespace totri

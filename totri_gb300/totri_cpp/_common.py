@@ -1,0 +1,30 @@
+"""Helpers shared by the drop-in ``totri_cpp`` functions."""
+import ctypes
+
+import torch
+
+from .. import _lib
+
+
+def dense_out(t):
+    """A C-contiguous tensor to write into (t itself when already dense)."""
+    return t if t.is_contiguous() else torch.empty_like(t, memory_format=torch.contiguous_format)
+
+
+def finish_out(t, out):
+    if out is not t:
+        t.copy_(out)
+
+
+def mesh_workspace(B, V, F, P, device):
+    """Scratch for one mesh call (BVH + visibility masks), from the caching allocator."""
+    n = int(_lib.load().totri_mesh_workspace(int(B), int(V), int(F), int(P)))
+    if n == 0:
+        return None
+    return torch.empty(n, dtype=torch.uint8, device=device)
+
+
+def ws_args(ws):
+    if ws is None:
+        return ctypes.c_void_p(None), 0
+    return ctypes.c_void_p(ws.data_ptr()), ws.numel()
