@@ -96,6 +96,24 @@ int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t*
                                 float bin_offset, int model, void* workspace,
                                 size_t workspace_bytes, void* stream);
 
+/* totri_mesh_confocal_forward without a caller-provided workspace. It has no
+ * counterpart in the reference. It exists for callers that cannot allocate
+ * device memory: hosts that own all device memory through a fixed pool,
+ * loops that must not pay the device synchronisation of an allocation, and
+ * foreign-language hosts that bind only this C ABI. Its scratch is one static
+ * 24 MiB device array inside the library (held on every GPU the library runs
+ * on until exit); inputs whose scratch would exceed it (see
+ * totri_mesh_workspace) fail with TOTRI_ERR_WORKSPACE before any work is
+ * enqueued. All calls share that array: calls that overlap on the GPU race
+ * and must be serialised by the caller. The first call on each device looks
+ * up the array's device address; make it before any stream capture. */
+int totri_mesh_confocal_forward_noalloc(const totri_array_t* verts, const totri_array_t* faces,
+                                        const totri_array_t* material,
+                                        const totri_array_t* scan_points,
+                                        const totri_array_t* scan_origin,
+                                        const totri_array_t* transient, float bin_width,
+                                        float bin_offset, int model, void* stream);
+
 /* Replaces totri_cpp.render.mesh_confocal_grad_verts
  * (src/render/mesh.h:20-29, src/render/mesh.cpp:22-36).
  * transient_grad [B,T,S]; verts_grad [B,V,3] or [B,V,0]; material_grad
