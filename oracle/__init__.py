@@ -48,6 +48,40 @@ _SIGNATURES = {
     "oracle_mesh_exhaustive_grad": (
         _int, [_f32p, _long, _i64p, _long, _f32p, _long, _f32p, _long, _f32p, _long, _f32p,
                _f32p, _u8p, _u8p, _long, _flt, _flt, _f64p, _int, _int, _f64p, _f64p]),
+    "oracle_volume_confocal_forward": (
+        _int, [_f32p, _int, _int, _int, _f32p, _int, _int, _f32p, _f32p, _flt, _flt, _int,
+               _f64p]),
+    "oracle_volume_confocal_adjoint": (
+        _int, [_f64p, _int, _int, _int, _f32p, _int, _int, _f32p, _f32p, _flt, _flt, _int,
+               _f64p]),
+    "oracle_volume_confocal_transposed": (
+        _int, [_f64p, _int, _int, _int, _f32p, _int, _int, _f32p, _f32p, _flt, _flt, _int,
+               _f64p]),
+    "oracle_volume_confocal_grad_mp": (
+        _int, [_f32p, _int, _int, _int, _f32p, _int, _int, _f64p, _f32p, _f32p, _flt, _flt,
+               _int, _f64p]),
+    "oracle_volume_exhaustive_forward": (
+        _int, [_f32p, _int, _int, _int, _f32p, _int, _f32p, _int, _int, _f32p, _f32p, _flt,
+               _flt, _int, _f64p]),
+    "oracle_volume_exhaustive_adjoint": (
+        _int, [_f64p, _int, _int, _int, _f32p, _int, _f32p, _int, _int, _f32p, _f32p, _flt,
+               _flt, _f64p]),
+    "oracle_bp_confocal_velten": (
+        _int, [_f32p, _int, _f32p, _int, _f32p, _int, _int, _int, _int, _f32p, _f32p, _flt,
+               _flt, _f64p]),
+    "oracle_bp_confocal_velten_adjoint": (
+        _int, [_f64p, _int, _int, _int, _f32p, _int, _f32p, _int, _int, _f32p, _f32p, _flt,
+               _flt, _f64p]),
+    "oracle_bp_exhaustive_velten": (
+        _int, [_f32p, _int, _f32p, _int, _f32p, _int, _f32p, _int, _f32p, _int, _int, _int,
+               _int, _f32p, _f32p, _flt, _flt, _f64p]),
+    "oracle_bp_exhaustive_arellano": (
+        _int, [_f32p, _int, _f32p, _int, _f32p, _int, _f32p, _int, _f32p, _int, _int, _int,
+               _int, _f32p, _f32p, _flt, _flt, _f64p]),
+    "oracle_rbf2volume_forward": (
+        _int, [_f32p, _int, _int, _int, _int, _int, _f32p, _f32p, _f64p]),
+    "oracle_rbf2volume_grad": (
+        _int, [_f32p, _int, _int, _int, _int, _int, _f64p, _f64p, _f32p, _f32p, _f64p]),
 }
 
 
@@ -196,3 +230,179 @@ def mesh_exhaustive_grad(verts, faces, material, scan_points, laser_points, scan
         ctypes.c_float(bin_width), ctypes.c_float(bin_offset), _ptr(tg, _f64p),
         int(want_verts), int(fp64), _ptr(vg, _f64p), _ptr(mg, _f64p))
     return vg, mg
+
+
+# ---------------------------------------------------------------------------
+# Volume renderer (one item; layouts as the reference's operators).
+
+def _v3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
+
+
+def _f64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def volume_confocal_forward(volume, mp, nbins, origin, size, bin_width, bin_offset, fp64=True):
+    """transient [N, T] of volume [X, Y, Z] seen from measurement points [3, N]."""
+    v, m = _f32(volume), _f32(mp)
+    o, s = _v3(origin), _v3(size)
+    out = np.zeros((m.shape[1], nbins), np.float64)
+    lib().oracle_volume_confocal_forward(_ptr(v, _f32p), *v.shape, _ptr(m, _f32p), m.shape[1],
+                                         nbins, _ptr(o, _f32p), _ptr(s, _f32p), bin_width,
+                                         bin_offset, int(fp64), _ptr(out, _f64p))
+    return out
+
+
+def volume_confocal_adjoint(transient, shape, mp, origin, size, bin_width, bin_offset,
+                            fp64=True):
+    """Exact adjoint of volume_confocal_forward: volume [X, Y, Z] from transient [N, T]."""
+    t, m = _f64(transient), _f32(mp)
+    o, s = _v3(origin), _v3(size)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_volume_confocal_adjoint(_ptr(t, _f64p), *shape, _ptr(m, _f32p), m.shape[1],
+                                         t.shape[1], _ptr(o, _f32p), _ptr(s, _f32p), bin_width,
+                                         bin_offset, int(fp64), _ptr(out, _f64p))
+    return out
+
+
+def volume_confocal_transposed(transient, shape, mp, origin, size, bin_width, bin_offset,
+                               fp64=True):
+    """The reference's transposed operator (volume_confocal_grad_volume)."""
+    t, m = _f64(transient), _f32(mp)
+    o, s = _v3(origin), _v3(size)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_volume_confocal_transposed(_ptr(t, _f64p), *shape, _ptr(m, _f32p), m.shape[1],
+                                            t.shape[1], _ptr(o, _f32p), _ptr(s, _f32p),
+                                            bin_width, bin_offset, int(fp64), _ptr(out, _f64p))
+    return out
+
+
+def volume_confocal_grad_mp(volume, mp, transient_grad, origin, size, bin_width, bin_offset,
+                            fp64=True):
+    """d loss / d measurement points [3, N]."""
+    v, m, g = _f32(volume), _f32(mp), _f64(transient_grad)
+    o, s = _v3(origin), _v3(size)
+    out = np.zeros((3, m.shape[1]), np.float64)
+    lib().oracle_volume_confocal_grad_mp(_ptr(v, _f32p), *v.shape, _ptr(m, _f32p), m.shape[1],
+                                         g.shape[1], _ptr(g, _f64p), _ptr(o, _f32p),
+                                         _ptr(s, _f32p), bin_width, bin_offset, int(fp64),
+                                         _ptr(out, _f64p))
+    return out
+
+
+def volume_exhaustive_forward(volume, scan_points, laser_points, nbins, start, end, bin_width,
+                              bin_offset):
+    """transient [T, S, L] of volume [D, H, W]; points [3, S] / [3, L]."""
+    v, sp, lp = _f32(volume), _f32(scan_points), _f32(laser_points)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros((nbins, sp.shape[1], lp.shape[1]), np.float64)
+    lib().oracle_volume_exhaustive_forward(_ptr(v, _f32p), *v.shape, _ptr(sp, _f32p),
+                                           sp.shape[1], _ptr(lp, _f32p), lp.shape[1], nbins,
+                                           _ptr(a, _f32p), _ptr(e, _f32p), bin_width, bin_offset,
+                                           1, _ptr(out, _f64p))
+    return out
+
+
+def volume_exhaustive_adjoint(transient_grad, shape, scan_points, laser_points, start, end,
+                              bin_width, bin_offset):
+    g, sp, lp = _f64(transient_grad), _f32(scan_points), _f32(laser_points)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_volume_exhaustive_adjoint(_ptr(g, _f64p), *shape, _ptr(sp, _f32p), sp.shape[1],
+                                           _ptr(lp, _f32p), lp.shape[1], g.shape[0],
+                                           _ptr(a, _f32p), _ptr(e, _f32p), bin_width, bin_offset,
+                                           _ptr(out, _f64p))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Backprojection (one item).
+
+def _origin(o, n):
+    if o is None:
+        return np.zeros((0, 3), np.float32), 0
+    o = _f32(o)
+    return o, o.shape[0] if o.ndim == 2 and o.shape[1] == 3 else o.shape[-1]
+
+
+def bp_confocal_velten(transient, scan_points, scan_origin, shape, start, end, bin_width,
+                       bin_offset):
+    """volume [D, H, W] from transient [T, S]; scan_points / scan_origin [S, 3]."""
+    t, sp = _f32(transient), _f32(scan_points)
+    so = _f32(scan_origin) if scan_origin is not None else np.zeros((0, 3), np.float32)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_bp_confocal_velten(_ptr(t, _f32p), t.shape[0], _ptr(sp, _f32p), sp.shape[0],
+                                    _ptr(so, _f32p), so.shape[0], *shape, _ptr(a, _f32p),
+                                    _ptr(e, _f32p), bin_width, bin_offset, _ptr(out, _f64p))
+    return out
+
+
+def bp_confocal_velten_adjoint(volume, scan_points, scan_origin, nbins, start, end, bin_width,
+                               bin_offset):
+    v, sp = _f64(volume), _f32(scan_points)
+    so = _f32(scan_origin) if scan_origin is not None else np.zeros((0, 3), np.float32)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros((nbins, sp.shape[0]), np.float64)
+    lib().oracle_bp_confocal_velten_adjoint(_ptr(v, _f64p), *v.shape, _ptr(sp, _f32p),
+                                            sp.shape[0], _ptr(so, _f32p), so.shape[0], nbins,
+                                            _ptr(a, _f32p), _ptr(e, _f32p), bin_width,
+                                            bin_offset, _ptr(out, _f64p))
+    return out
+
+
+def bp_exhaustive_velten(transient, scan_points, laser_points, scan_origin, laser_origin, shape,
+                         start, end, bin_width, bin_offset):
+    """volume [D, H, W] from transient [T, S, L]; points [S, 3] / [L, 3]."""
+    t, sp, lp = _f32(transient), _f32(scan_points), _f32(laser_points)
+    so = _f32(scan_origin) if scan_origin is not None else np.zeros((0, 3), np.float32)
+    lo = _f32(laser_origin) if laser_origin is not None else np.zeros((0, 3), np.float32)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_bp_exhaustive_velten(_ptr(t, _f32p), t.shape[0], _ptr(sp, _f32p), sp.shape[0],
+                                      _ptr(lp, _f32p), lp.shape[0], _ptr(so, _f32p),
+                                      so.shape[0], _ptr(lo, _f32p), lo.shape[0], *shape,
+                                      _ptr(a, _f32p), _ptr(e, _f32p), bin_width, bin_offset,
+                                      _ptr(out, _f64p))
+    return out
+
+
+def bp_exhaustive_arellano(transient, scan_points, laser_points, scan_origin, laser_origin,
+                           shape, start, end, bin_width, bin_offset):
+    """volume [D, H, W] from transient [T, S, L]; points [3, S] / [3, L] (origins [3, n])."""
+    t, sp, lp = _f32(transient), _f32(scan_points), _f32(laser_points)
+    so = _f32(scan_origin) if scan_origin is not None else np.zeros((3, 0), np.float32)
+    lo = _f32(laser_origin) if laser_origin is not None else np.zeros((3, 0), np.float32)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros(tuple(shape), np.float64)
+    lib().oracle_bp_exhaustive_arellano(_ptr(t, _f32p), t.shape[0], _ptr(sp, _f32p), sp.shape[1],
+                                        _ptr(lp, _f32p), lp.shape[1], _ptr(so, _f32p),
+                                        so.shape[1], _ptr(lo, _f32p), lo.shape[1], *shape,
+                                        _ptr(a, _f32p), _ptr(e, _f32p), bin_width, bin_offset,
+                                        _ptr(out, _f64p))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# RBF to volume (one item).
+
+def rbf2volume_forward(rbf, shape, start, end):
+    """volume [1+A, D, H, W] from rbf [N, 4+A]."""
+    r = _f32(rbf)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros((r.shape[1] - 3,) + tuple(shape), np.float64)
+    lib().oracle_rbf2volume_forward(_ptr(r, _f32p), r.shape[0], r.shape[1], *shape,
+                                    _ptr(a, _f32p), _ptr(e, _f32p), _ptr(out, _f64p))
+    return out
+
+
+def rbf2volume_grad(rbf, volume, volume_grad, start, end):
+    """rbf_grad [N, 4+A]."""
+    r, v, g = _f32(rbf), _f64(volume), _f64(volume_grad)
+    a, e = _v3(start), _v3(end)
+    out = np.zeros(r.shape, np.float64)
+    lib().oracle_rbf2volume_grad(_ptr(r, _f32p), r.shape[0], r.shape[1], *v.shape[1:],
+                                 _ptr(v, _f64p), _ptr(g, _f64p), _ptr(a, _f32p), _ptr(e, _f32p),
+                                 _ptr(out, _f64p))
+    return out
