@@ -180,25 +180,46 @@ __device__ __forceinline__ float safe_inv(float d) {
   return fabsf(d) < 1e-20f ? copysignf(1e20f, d) : 1.f / d;
 }
 
-// True when face k (sorted position) is the closest hit, lowest face index on
-// ties, of the ray from o to its centroid within [0, 1.01 d + 1e-3]
-// (mesh_confocal_forward_optix.cu:42-65). brute: test every face instead of
-// walking the BVH (same answer by construction).
+// The target of a visibility query: face k (Morton position) with its
+// intersection record and centroid, loaded once for many wall points.
+struct Target {
+  int k, f;
+  float4 a0, a1, a2, a3;
+  fv3 c;
+};
+
+__device__ __forceinline__ Target load_target(const Scene& sc, int b, int k) {
+  Target t;
+  t.k = k;
+  const float4* tr = tri_at(sc, b, k);
+  t.a0 = __ldg(tr);
+  t.a1 = __ldg(tr + 1);
+  t.a2 = __ldg(tr + 2);
+  t.a3 = __ldg(tr + 3);
+  t.f = __float_as_int(t.a3.w);
+  const float4 c4 = __ldg(shade_at(sc, b, k) + 3);
+  t.c = mkv(c4.x, c4.y, c4.z);
+  return t;
+}
+
+// True when the target face is the closest hit, lowest face index on ties, of
+// the ray from o to its centroid within [0, 1.01 d + 1e-3]
+// (mesh_confocal_forward_optix.cu:42-65). Any single occluder settles "not
+// visible", so `cache` (a Morton position or -1) is tested first: callers pass
+// the occluder found for a neighbouring wall point. kBrute tests every face
+// instead of walking the BVH; the answer is the same by construction.
 template <bool kBrute>
-__device__ bool face_visible(const Scene& sc, int b, int n, int k, fv3 o, uint32_t* status) {
-  const float4* sr = shade_at(sc, b, k);
-  const float4 c4 = __ldg(sr + 3);
-  const fv3 c = mkv(c4.x, c4.y, c4.z);
-  const fv3 D = xsub3(c, o);
+__device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, fv3 o, int& cache,
+                               uint32_t* status) {
+  const int k = tg.k;
+  const fv3 D = xsub3(tg.c, o);
   const float dist = xlen(D);
   if (!(dist >= 1e-6f)) return false;
   const fv3 dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
   const float tmax = xadd(xmul(dist, 1.01f), 1e-3f);
-  const float4* tr = tri_at(sc, b, k);
-  const float4 a0 = __ldg(tr), a1 = __ldg(tr + 1), a2 = __ldg(tr + 2), a3 = __ldg(tr + 3);
-  const int f = __float_as_int(a3.w);
+  const int f = tg.f;
   float tf;
-  if (!tri_hit(a0, a1, a2, a3, o, dir, tmax, tf)) return false;
+  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return false;
 
   auto occludes = [&](int kk) -> bool {
     if (kk == k) return false;
@@ -208,14 +229,16 @@ __device__ bool face_visible(const Scene& sc, int b, int n, int k, fv3 o, uint32
     }
     const float4* q = tri_at(sc, b, kk);
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
-    float tg;
-    if (!tri_hit(q0, q1, q2, q3, o, dir, tmax, tg)) return false;
-    return tg < tf || (tg == tf && __float_as_int(q3.w) < f);
+    float tq;
+    if (!tri_hit(q0, q1, q2, q3, o, dir, tmax, tq)) return false;
+    return tq < tf || (tq == tf && __float_as_int(q3.w) < f);
   };
+
+  if (cache >= 0 && occludes(cache)) return false;
 
   if (kBrute || n == 1) {
     for (int kk = 0; kk < n; ++kk)
-      if (occludes(kk)) return false;
+      if (occludes(kk)) { cache = kk; return false; }
     return true;
   }
 
@@ -234,11 +257,11 @@ __device__ bool face_visible(const Scene& sc, int b, int n, int k, fv3 o, uint32
     bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
     const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
     if (h0 && c0 < 0) {
-      if (occludes(~c0)) return false;
+      if (occludes(~c0)) { cache = ~c0; return false; }
       h0 = false;
     }
     if (h1 && c1 < 0) {
-      if (occludes(~c1)) return false;
+      if (occludes(~c1)) { cache = ~c1; return false; }
       h1 = false;
     }
     if (h0 && h1) {

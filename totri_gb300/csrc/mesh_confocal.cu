@@ -23,6 +23,9 @@ namespace mesh {
 
 namespace {
 
+// One warp per (wall point, 32 Morton-consecutive faces): the 32 rays share
+// their origin and end on a compact patch of the surface, so they walk
+// largely the same BVH nodes.
 template <bool kBrute>
 __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
   const int lane = threadIdx.x & 31;
@@ -38,7 +41,8 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
   bool vis = false;
   if (k < n) {
     const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
-    vis = face_visible<kBrute>(sc, b, n, k, o, sc.status);
+    int cache = -1;
+    vis = target_visible<kBrute>(sc, b, n, load_target(sc, b, k), o, cache, sc.status);
   }
   const uint32_t word = __ballot_sync(0xffffffffu, vis);
   if (lane == 0) sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
