@@ -201,15 +201,22 @@ int totri_mesh_workspace_status(const void* workspace, size_t workspace_bytes,
 /* ----------------------------------------------------------------------- */
 /* render: volumes                                                          */
 
+/* Scratch bytes for the volume entry points that list occupied voxels
+ * (confocal forward, measurement-point gradient, exhaustive forward):
+ * num_voxels = X*Y*Z (or D*H*W of one batch item). */
+size_t totri_volume_workspace(int64_t num_voxels);
+
 /* Replaces totri_cpp.render.volume_confocal_forward
  * (src/render/volume.h:10-16, src/render/volume.cpp:7-23).
  * volume [X,Y,Z], measurement_points [3,N], transient [N,T] (overwritten);
- * volume_origin/volume_size are 3-vectors. f32 or f64 (all the same). */
+ * volume_origin/volume_size are 3-vectors. float32 (the reference also
+ * dispatches float64; that is refused with TOTRI_ERR_UNSUPPORTED). */
 int totri_volume_confocal_forward(const totri_array_t* volume,
                                   const totri_array_t* measurement_points,
                                   const totri_array_t* transient, const float volume_origin[3],
                                   const float volume_size[3], float bin_width,
-                                  float bin_offset, void* stream);
+                                  float bin_offset, void* workspace, size_t workspace_bytes,
+                                  void* stream);
 
 /* Replaces totri_cpp.render.volume_confocal_grad_volume
  * (src/render/volume.h:18-24, src/render/volume.cpp:25-41): the transposed
@@ -237,7 +244,7 @@ int totri_volume_confocal_grad_measurement_points(
     const totri_array_t* measurement_points_grad, const totri_array_t* volume,
     const totri_array_t* measurement_points, const totri_array_t* transient_grad,
     const float volume_origin[3], const float volume_size[3], float bin_width,
-    float bin_offset, void* stream);
+    float bin_offset, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Replaces totri_cpp.render.volume_render_exhaustive_forward
  * (src/render/volume.h:34-43, src/render/volume.cpp:83-96).
@@ -251,7 +258,8 @@ int totri_volume_exhaustive_forward(const totri_array_t* volume,
                                     const totri_array_t* laser_origin,
                                     const totri_array_t* transient,
                                     const float volume_start[3], const float volume_end[3],
-                                    float bin_width, float bin_offset, void* stream);
+                                    float bin_width, float bin_offset, void* workspace,
+                                    size_t workspace_bytes, void* stream);
 
 /* Replaces totri_cpp.render.volume_render_exhaustive_grad_volume
  * (src/render/volume.h:45-54, src/render/volume.cpp:98-111), whose kernel

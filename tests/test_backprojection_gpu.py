@@ -1,0 +1,99 @@
+"""Backprojection on the GPU against the FP64 oracle and the reference's golden
+vectors; the Velten adjoint against <B x, y> = <x, B^T y>.
+
+Tolerances (rel-L2): 1e-5 vs the FP64 oracle, 1e-4 vs the reference's FP32
+outputs (nearest-bin decisions are shared, so these are summation-order
+differences only).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from totri_gb300 import scenes
+from totri_gb300.reconstruct import (BackprojectionConfocalVelten,
+                                     BackprojectionExhaustiveArellano,
+                                     BackprojectionExhaustiveVelten)
+from totri_gb300.totri_cpp import reconstruct as K
+from totri_gb300.types import BinDef, VolumeDef
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def cu(a):
+    return torch.as_tensor(np.ascontiguousarray(a)).cuda()
+
+
+def test_golden_vectors(cuda_lib):
+    g = dict(np.load(os.path.join(GOLDEN, "backprojection.npz")))
+    shape = tuple(int(x) for x in g["shape"])
+    vd = VolumeDef(tuple(g["start"].tolist()), tuple(g["end"].tolist()), shape)
+    v = BackprojectionConfocalVelten.apply(cu(g["transient_confocal"]), cu(g["scan_points"]), vd,
+                                           BinDef(0.02, 0.0), cu(g["scan_origin"]))
+    assert rel(v.cpu().numpy(), g["volume_confocal"]) < 1e-4
+    v = BackprojectionExhaustiveVelten.apply(cu(g["transient_exhaustive"]), cu(g["scan_points"]),
+                                             cu(g["laser_points"]), vd, BinDef(0.01, 0.0))
+    assert rel(v.cpu().numpy(), g["volume_exhaustive"]) < 1e-4
+    v = BackprojectionExhaustiveArellano.apply(
+        cu(g["transient_exhaustive"]), cu(g["scan_points"].transpose(0, 2, 1)),
+        cu(g["laser_points"].transpose(0, 2, 1)), vd, BinDef(0.01, 0.0))
+    assert rel(v.cpu().numpy(), g["volume_arellano"]) < 1e-4
+
+
+def test_against_oracle_with_origins(cuda_lib):
+    rng = np.random.default_rng(7)
+    S, L, T, shape = 40, 5, 100, (7, 8, 9)
+    st, en = (-0.5, -0.5, 0.5), (0.5, 0.5, 1.5)
+    sp = np.stack([rng.uniform(-1, 1, S), rng.uniform(-1, 1, S), np.zeros(S)], 1).astype(np.float32)
+    lp = np.stack([rng.uniform(-1, 1, L), rng.uniform(-1, 1, L), np.zeros(L)], 1).astype(np.float32)
+    so = np.tile(np.array([[0.1, 0.2, -1.5]], np.float32), (S, 1))
+    lo = np.tile(np.array([[-0.3, 0.0, -1.0]], np.float32), (L, 1))
+    trc = rng.random((1, T, S)).astype(np.float32)
+    tre = rng.random((1, T, S, L)).astype(np.float32)
+    vd = VolumeDef(st, en, shape)
+    v = BackprojectionConfocalVelten.apply(cu(trc), cu(sp[None]), vd, BinDef(0.02, 0.05),
+                                           cu(so[None]))
+    ref = oracle.bp_confocal_velten(trc[0], sp, so, shape, st, en, 0.02, 0.05)
+    assert rel(v[0].cpu().numpy(), ref) < 1e-5
+    v = BackprojectionExhaustiveVelten.apply(cu(tre), cu(sp[None]), cu(lp[None]), vd,
+                                             BinDef(0.01, 0.0), cu(so[None]), cu(lo[None]))
+    ref = oracle.bp_exhaustive_velten(tre[0], sp, lp, so, lo, shape, st, en, 0.01, 0.0)
+    assert rel(v[0].cpu().numpy(), ref) < 1e-5
+    v = BackprojectionExhaustiveArellano.apply(cu(tre), cu(sp.T[None]), cu(lp.T[None]), vd,
+                                               BinDef(0.01, 0.0), cu(so.T[None]), cu(lo.T[None]))
+    ref = oracle.bp_exhaustive_arellano(tre[0], sp.T, lp.T, so.T, lo.T, shape, st, en, 0.01, 0.0)
+    assert rel(v[0].cpu().numpy(), ref) < 1e-5
+
+
+def test_velten_adjoint_full_size(cuda_lib):
+    """128^3 voxels x 128x128 scan points x 1024 bins: <B x, y> = <x, B^T y>, and
+    the forward against the oracle on a 64-point subset of the scan."""
+    s = scenes.volume_scene()
+    vd, bd = s["volume_def"], s["bin_def"]
+    sp = s["scan_points"].cuda()
+    S = sp.shape[1]
+    x = torch.rand((1, bd.num, S), device="cuda")
+    bx = BackprojectionConfocalVelten.apply(x, sp, vd, bd)
+    y = torch.randn_like(bx)
+    bty = torch.empty_like(x)
+    K.backprojection_confocal_velten_adjoint(y, sp, torch.empty_like(sp[:, :0]), bty, vd.start,
+                                             vd.end, bd.width, bd.offset)
+    lhs = float((bx.double() * y.double()).sum())
+    rhs = float((x.double() * bty.double()).sum())
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+    sub = np.linspace(0, S - 1, 64).astype(np.int64)
+    xs = x[:, :, sub].contiguous()
+    v = BackprojectionConfocalVelten.apply(xs, sp[:, sub].contiguous(), vd, bd)
+    ref = oracle.bp_confocal_velten(xs[0].cpu().numpy(), sp[0, sub].cpu().numpy(), None,
+                                    vd.resolution, vd.start, vd.end, bd.width, bd.offset)
+    assert rel(v[0].cpu().numpy(), ref) < 1e-5

@@ -129,6 +129,28 @@ def test_visibility_occluder_blocks():
     assert oracle.mesh_count_faces(faces_pad, 7) == 1
 
 
+def test_rbf_gradient_matches_fp64_central_differences():
+    """RBF gradient formula vs central differences of the FP64 forward (h = 1e-4)."""
+    rng = np.random.default_rng(9)
+    N = 5
+    rbf = np.concatenate([rng.uniform(-0.3, 0.3, (N, 3)) + np.array([0, 0, 1.0]),
+                          rng.uniform(0.1, 0.2, (N, 1)), rng.random((N, 1))], 1)
+    rbf = rbf.astype(np.float32).astype(np.float64)
+    shape, st, en = (6, 5, 4), (-0.5, -0.5, 0.5), (0.5, 0.5, 1.5)
+    w = rng.standard_normal((2,) + shape)
+    vol = oracle.rbf2volume_forward(rbf, shape, st, en)
+    g = oracle.rbf2volume_grad(rbf, vol, w, st, en)
+    for i in range(N):
+        for c in range(5):
+            rp, rm = rbf.copy(), rbf.copy()
+            rp[i, c] = np.float32(rbf[i, c] + 1e-4)
+            rm[i, c] = np.float32(rbf[i, c] - 1e-4)
+            h = float(rp[i, c]) - float(rm[i, c])
+            fd = ((w * oracle.rbf2volume_forward(rp, shape, st, en)).sum() -
+                  (w * oracle.rbf2volume_forward(rm, shape, st, en)).sum()) / h
+            assert abs(fd - g[i, c]) <= 1e-3 * max(1.0, abs(g[i, c])), (i, c, fd, g[i, c])
+
+
 @pytest.mark.parametrize("kind", ["confocal", "exhaustive"])
 def test_mesh_gradient_matches_fp64_central_differences(kind):
     """The restated gradient formula against central differences of the FP64

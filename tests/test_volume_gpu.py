@@ -1,0 +1,148 @@
+"""Volume renderer on the GPU against the FP64 oracle, the reference's golden
+vectors, and the adjoint identity <A x, y> = <x, A^T y>.
+
+Tolerances (rel-L2): forwards/adjoints 1e-5 vs the FP64 oracle; 1e-4 vs the
+reference's FP32 outputs; measurement-point gradient 1e-4 vs the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from totri_gb300 import scenes
+from totri_gb300.render import VolumeRenderConfocal, VolumeRenderExhaustive
+from totri_gb300.totri_cpp import render as R
+from totri_gb300.types import BinDef, VolumeDef
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def cu(a):
+    return torch.as_tensor(np.ascontiguousarray(a)).cuda()
+
+
+def small_case(seed=0, X=12, N=40, T=96):
+    g = np.random.default_rng(seed)
+    vol = ((g.random((X, X, X)) < 0.1) * g.random((X, X, X))).astype(np.float32)
+    mp = np.stack([g.uniform(-1, 1, N), g.uniform(-1, 1, N), np.zeros(N)]).astype(np.float32)
+    return vol, mp, (-0.5, -0.5, 0.5), (1.0, 1.0, 1.0), T, 0.03, 0.0
+
+
+def test_confocal_forward_adjoint_and_points_grad(cuda_lib):
+    vol, mp, org, size, T, bw, bo = small_case()
+    out = torch.full((mp.shape[1], T), 3.0, device="cuda")
+    R.volume_confocal_forward(cu(vol), cu(mp), out, org, size, bw, bo)
+    ref = oracle.volume_confocal_forward(vol, mp, T, org, size, bw, bo)
+    assert rel(out.cpu().numpy(), ref) < 1e-5
+    y = np.random.default_rng(1).standard_normal((mp.shape[1], T)).astype(np.float32)
+    adj = torch.empty(vol.shape, device="cuda")
+    R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+    assert rel(adj.cpu().numpy(), oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw,
+                                                                 bo)) < 1e-5
+    tr = torch.empty(vol.shape, device="cuda")
+    R.volume_confocal_grad_volume(tr, cu(mp), cu(y), org, size, bw, bo)
+    assert rel(tr.cpu().numpy(),
+               oracle.volume_confocal_transposed(y, vol.shape, mp, org, size, bw, bo)) < 1e-5
+    gm = torch.empty((3, mp.shape[1]), device="cuda")
+    R.volume_confocal_grad_measurement_points(gm, cu(vol), cu(mp), cu(y), org, size, bw, bo)
+    assert rel(gm.cpu().numpy(), oracle.volume_confocal_grad_mp(vol, mp, y, org, size, bw,
+                                                                bo)) < 1e-4
+
+
+def test_confocal_matches_reference_golden(cuda_lib):
+    g = dict(np.load(os.path.join(GOLDEN, "volume_confocal.npz")))
+    T, bw, bo = int(g["bin"][0]), float(g["bin"][1]), float(g["bin"][2])
+    out = torch.empty((g["mp"].shape[1], T), device="cuda")
+    R.volume_confocal_forward(cu(g["volume"]), cu(g["mp"]), out, g["origin"], g["size"], bw, bo)
+    assert rel(out.cpu().numpy(), g["transient"]) < 1e-4
+    tv = torch.empty(g["volume"].shape, device="cuda")
+    R.volume_confocal_grad_volume(tv, cu(g["mp"]), cu(g["transient_grad"]), g["origin"],
+                                  g["size"], bw, bo)
+    assert rel(tv.cpu().numpy(), g["grad_volume"]) < 1e-4
+    gm = torch.empty_like(cu(g["mp"]))
+    R.volume_confocal_grad_measurement_points(gm, cu(g["volume"]), cu(g["mp"]),
+                                              cu(g["transient_grad"]), g["origin"], g["size"],
+                                              bw, bo)
+    assert rel(gm.cpu().numpy(), g["grad_mp"]) < 1e-4
+
+
+def test_confocal_autograd_uses_exact_adjoint(cuda_lib):
+    vol, mp, org, size, T, bw, bo = small_case(seed=2)
+    v = cu(vol).requires_grad_(True)
+    p = cu(mp).requires_grad_(True)
+    tr = VolumeRenderConfocal.apply(v, p, org, size, T, bw, bo)
+    w = torch.randn_like(tr)
+    (tr * w).sum().backward()
+    adj = oracle.volume_confocal_adjoint(w.cpu().numpy(), vol.shape, mp, org, size, bw, bo)
+    assert rel(v.grad.cpu().numpy(), adj) < 1e-5
+    assert p.grad is not None and torch.isfinite(p.grad).all()
+
+
+def test_confocal_full_size_adjoint_identity_and_sampled_points(cuda_lib):
+    """128^3 voxels (2% occupied), 128x128 scan points, 1024 bins: the adjoint
+    identity on the whole operator (FP64 reductions), and 12 transient rows
+    against the FP64 oracle."""
+    s = scenes.volume_scene()
+    vd, bd = s["volume_def"], s["bin_def"]
+    org = vd.start
+    size = tuple(e - a for a, e in zip(vd.start, vd.end))
+    vol = s["volume"].cuda()
+    mp = s["scan_points"][0].T.contiguous().cuda()
+    N, T = mp.shape[1], bd.num
+    out = torch.empty((N, T), device="cuda")
+    R.volume_confocal_forward(vol, mp, out, org, size, bd.width, bd.offset)
+    y = torch.randn((N, T), device="cuda")
+    adj = torch.empty_like(vol)
+    R.volume_confocal_adjoint(adj, mp, y, org, size, bd.width, bd.offset)
+    lhs = (out.double() * y.double()).sum().item()
+    rhs = (vol.double() * adj.double()).sum().item()
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+    rows = np.random.default_rng(3).choice(N, 12, replace=False)
+    ref = oracle.volume_confocal_forward(s["volume"].numpy(), mp[:, rows].cpu().numpy(), T, org,
+                                         size, bd.width, bd.offset)
+    assert rel(out[rows].cpu().numpy(), ref) < 1e-5
+
+
+def exhaustive_case(seed=4):
+    g = np.random.default_rng(seed)
+    D, H, W, S, L, T = 6, 5, 7, 9, 4, 64
+    vol = ((g.random((1, D, H, W)) < 0.3) * g.random((1, D, H, W))).astype(np.float32)
+    sp = np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S), np.zeros(S)])[None].astype(np.float32)
+    lp = np.stack([g.uniform(-1, 1, L), g.uniform(-1, 1, L), np.zeros(L)])[None].astype(np.float32)
+    return vol, sp, lp, T, (-0.5, -0.5, 0.5), (0.5, 0.5, 1.5), 0.05
+
+
+def test_exhaustive_forward_and_adjoint(cuda_lib):
+    vol, sp, lp, T, st, en, bw = exhaustive_case()
+    vd = VolumeDef(st, en, vol.shape[1:])
+    bd = BinDef(bw, 0.0, T)
+    v = cu(vol).requires_grad_(True)
+    tr = VolumeRenderExhaustive.apply(v, cu(sp), cu(lp), vd, bd)
+    ref = oracle.volume_exhaustive_forward(vol[0], sp[0], lp[0], T, st, en, bw, 0.0)
+    assert rel(tr[0].detach().cpu().numpy(), ref) < 1e-5
+    g = dict(np.load(os.path.join(GOLDEN, "volume_exhaustive.npz")))
+    out = torch.empty(g["transient"].shape, device="cuda")
+    empty = torch.empty((1, 3, 0), device="cuda")
+    R.volume_render_exhaustive_forward(cu(g["volume"]), cu(g["scan_points"]),
+                                       cu(g["laser_points"]), empty, empty, out, g["start"],
+                                       g["end"], float(g["bin"][1]), float(g["bin"][2]))
+    assert rel(out.cpu().numpy(), g["transient"]) < 1e-4
+    w = torch.randn_like(tr)
+    (tr * w).sum().backward()
+    adj = oracle.volume_exhaustive_adjoint(w[0].cpu().numpy(), vol.shape[1:], sp[0], lp[0], st,
+                                           en, bw, 0.0)
+    assert rel(v.grad[0].cpu().numpy(), adj) < 1e-5
+    # adjoint identity
+    lhs = float((tr.detach().double() * w.double()).sum())
+    rhs = float((v.detach().double() * v.grad.double()).sum())
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)

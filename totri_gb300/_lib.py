@@ -66,11 +66,13 @@ _SIGNATURES = {
     "totri_mesh_exhaustive_grad_verts_reuse": [_ArrP] * 10 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_visibility": [_ArrP] * 4 + [_int, _vp, _sz, _vp],
     "totri_mesh_workspace_status": [_vp, _sz, ctypes.POINTER(ctypes.c_uint32), _vp],
-    "totri_volume_confocal_forward": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp],
+    "totri_volume_workspace": [_i64],
+    "totri_volume_confocal_forward": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp, _sz, _vp],
     "totri_volume_confocal_grad_volume": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp],
     "totri_volume_confocal_adjoint": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp],
-    "totri_volume_confocal_grad_measurement_points": [_ArrP] * 4 + [_F3, _F3, _flt, _flt, _vp],
-    "totri_volume_exhaustive_forward": [_ArrP] * 6 + [_F3, _F3, _flt, _flt, _vp],
+    "totri_volume_confocal_grad_measurement_points": [_ArrP] * 4 + [_F3, _F3, _flt, _flt, _vp,
+                                                                    _sz, _vp],
+    "totri_volume_exhaustive_forward": [_ArrP] * 6 + [_F3, _F3, _flt, _flt, _vp, _sz, _vp],
     "totri_volume_exhaustive_grad_volume": [_ArrP] * 6 + [_F3, _F3, _flt, _flt, _vp],
     "totri_backprojection_confocal_velten_forward": [_ArrP] * 4 + [_F3, _F3, _flt, _flt, _vp],
     "totri_backprojection_confocal_velten_adjoint": [_ArrP] * 4 + [_F3, _F3, _flt, _flt, _vp],
@@ -84,6 +86,7 @@ _RESTYPES = {
     "totri_version": ctypes.c_char_p,
     "totri_last_error": ctypes.c_char_p,
     "totri_mesh_workspace": ctypes.c_size_t,
+    "totri_volume_workspace": ctypes.c_size_t,
     "totri_profile_reset": None,
 }
 

@@ -1,0 +1,400 @@
+// Backprojection reconstructions: Velten confocal (and its adjoint), Velten
+// exhaustive, Arellano exhaustive.
+//
+// Reference: src/reconstruct/backprojection_cuda.cu (:153-194 Velten
+// confocal, :229-287 Velten exhaustive, :11-115 Arellano). The Velten kernels
+// gather per voxel; here a CTA of 256 voxels stages scan points (and their
+// wall-to-origin distances) in shared memory in tiles, so each scan point is
+// read once per CTA rather than once per voxel. The adjoint owns a tile of
+// scan points and keeps their transient columns in shared memory.
+#include <string>
+
+#include "capi_common.cuh"
+
+namespace totri {
+namespace bp {
+
+struct Grid {
+  int D, H, W;
+  float sx, sy, sz, ex, ey, ez;
+};
+
+// start + (i / (n - 1)) * (end - start) (backprojection_cuda.cu:167-170).
+__device__ __forceinline__ float grid_coord(float s, float e, int n, int i) {
+  return xadd(s, xmul(xdiv((float)i, (float)(n - 1)), xsub(e, s)));
+}
+
+__device__ __forceinline__ fv3 voxel_point(const Grid& g, int x, int y, int z) {
+  return mkv(grid_coord(g.sx, g.ex, g.W, x), grid_coord(g.sy, g.ey, g.H, y),
+             grid_coord(g.sz, g.ez, g.D, z));
+}
+
+// floor((dist - offset) / width + 0.5) (backprojection_cuda.cu:187).
+__device__ __forceinline__ int nearest_bin(float dist, float bw, float bo) {
+  const float b = floorf(xadd(xdiv(xsub(dist, bo), bw), 0.5f));
+  if (!(b == b)) return -1;
+  if (b > 2.0e9f) return 2000000000;
+  if (b < -2.0e9f) return -2000000000;
+  return (int)b;
+}
+
+struct Pts3 {  // [B, n, 3] with strides
+  const float* p;
+  int64_t sb, sn, sc;
+  __device__ fv3 at(int b, int i) const {
+    const float* q = p + b * sb + i * sn;
+    return mkv(q[0], q[sc], q[2 * sc]);
+  }
+};
+
+constexpr int kTile = 512;
+
+__global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int T, int S,
+                                                              Pts3 sp, Pts3 so, int has_origin,
+                                                              float bw, float bo,
+                                                              const float* __restrict__ tr,
+                                                              float* __restrict__ vol) {
+  __shared__ float4 pts[kTile];  // scan point xyz, 2 * |scan - origin|
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((int64_t)g.W * g.H));
+  const fv3 p = voxel_point(g, x, y, z);
+  const float* trb = tr + (size_t)b * T * S;
+  float value = 0.f;
+  for (int s0 = 0; s0 < S; s0 += kTile) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < kTile && s0 + j < S; j += blockDim.x) {
+      const fv3 q = sp.at(b, s0 + j);
+      const float od = has_origin ? xlen(xsub3(q, so.at(b, s0 + j))) : 0.f;
+      pts[j] = make_float4(q.x, q.y, q.z, xmul(2.f, od));
+    }
+    __syncthreads();
+    if (v < nv) {
+      const int cnt = min(kTile, S - s0);
+      for (int j = 0; j < cnt; ++j) {
+        const float4 q = pts[j];
+        const float sv = xlen(xsub3(mkv(q.x, q.y, q.z), p));
+        const int t = nearest_bin(xadd(q.w, xmul(2.f, sv)), bw, bo);
+        if (t >= 0 && t < T) value += __ldg(trb + (size_t)t * S + s0 + j);
+      }
+    }
+  }
+  if (v < nv) vol[(size_t)b * nv + v] = value;
+}
+
+// Adjoint: transient [T, S] tile of TS scan points in shared memory, all voxels.
+constexpr int kTS = 8;
+__global__ void __launch_bounds__(256) velten_adjoint_kernel(Grid g, int b, int T, int S, Pts3 sp,
+                                                             Pts3 so, int has_origin, float bw,
+                                                             float bo,
+                                                             const float* __restrict__ vol,
+                                                             float* __restrict__ tr) {
+  extern __shared__ float hist[];  // [T][kTS]
+  const int s0 = blockIdx.x * kTS;
+  for (int j = threadIdx.x; j < T * kTS; j += blockDim.x) hist[j] = 0.f;
+  __syncthreads();
+  const int sl = threadIdx.x % kTS;
+  const int s = s0 + sl;
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  if (s < S) {
+    const fv3 q = sp.at(b, s);
+    const float od2 = xmul(2.f, has_origin ? xlen(xsub3(q, so.at(b, s))) : 0.f);
+    const float* vb = vol + (size_t)b * nv;
+    for (int64_t v = threadIdx.x / kTS; v < nv; v += blockDim.x / kTS) {
+      const float val = __ldg(vb + v);
+      if (val == 0.f) continue;
+      const int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((int64_t)g.W * g.H));
+      const float sv = xlen(xsub3(q, voxel_point(g, x, y, z)));
+      const int t = nearest_bin(xadd(od2, xmul(2.f, sv)), bw, bo);
+      if (t >= 0 && t < T) atomicAdd(hist + t * kTS + sl, val);
+    }
+  }
+  __syncthreads();
+  float* out = tr + (size_t)b * T * S;
+  for (int j = threadIdx.x; j < T * kTS; j += blockDim.x) {
+    const int t = j / kTS, c = j - t * kTS;
+    if (s0 + c < S) out[(size_t)t * S + s0 + c] = hist[j];
+  }
+}
+
+__global__ void __launch_bounds__(128) velten_exhaustive_kernel(Grid g, int b, int T, int S, int L,
+                                                                Pts3 sp, Pts3 lp, Pts3 so, Pts3 lo,
+                                                                int has_so, int has_lo, float bw,
+                                                                float bo,
+                                                                const float* __restrict__ tr,
+                                                                float* __restrict__ vol) {
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((int64_t)g.W * g.H));
+  const fv3 p = voxel_point(g, x, y, z);
+  const float* trb = tr + (size_t)b * T * S * L;
+  float value = 0.f;
+  for (int s = 0; s < S; ++s) {
+    const fv3 q = sp.at(b, s);
+    const float sv = xlen(xsub3(q, p));
+    const float sod = has_so ? xlen(xsub3(q, so.at(b, s))) : 0.f;
+    const float a = xadd(sod, sv);
+    for (int l = 0; l < L; ++l) {
+      const fv3 r = lp.at(b, l);
+      const float lv = xlen(xsub3(r, p));
+      const float lod = has_lo ? xlen(xsub3(r, lo.at(b, l))) : 0.f;
+      const int t = nearest_bin(xadd(xadd(a, lv), lod), bw, bo);
+      if (t >= 0 && t < T) value += __ldg(trb + ((size_t)t * S + s) * L + l);
+    }
+  }
+  vol[(size_t)b * nv + v] = value;
+}
+
+struct Pts3T {  // [B, 3, n] with strides
+  const float* p;
+  int64_t sb, sc, sn;
+  __device__ fv3 at(int b, int i) const {
+    const float* q = p + b * sb + i * sn;
+    return mkv(q[0], q[sc], q[2 * sc]);
+  }
+};
+
+// Arellano (backprojection_cuda.cu:11-115): per (column, scan, laser), scale
+// the ellipsoid of constant path length to a sphere along the scan-laser axis
+// and deposit each positive bin where the column's ray meets it. int()
+// truncation makes the reference's interpolation weight always 0 (nearest).
+__global__ void __launch_bounds__(64) arellano_kernel(Grid g, int b, int T, int S, int L, Pts3T sp,
+                                                      Pts3T lp, Pts3T so, Pts3T lo, int has_so,
+                                                      int has_lo, float bw, float bo,
+                                                      const float* __restrict__ tr,
+                                                      float* __restrict__ vol) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y, l = blockIdx.z;
+  if (c >= g.H * g.W) return;
+  const int xi = c % g.W, yi = c / g.W;
+  const float xf = xadd(g.sx, xmul(xdiv((float)xi, (float)(g.W - 1)), xsub(g.ex, g.sx)));
+  const float yf = xadd(g.sy, xmul(xdiv((float)yi, (float)(g.H - 1)), xsub(g.ey, g.sy)));
+  const fv3 sc = sp.at(b, s), lc = lp.at(b, l);
+  const float sd = has_so ? xlen(xsub3(sc, so.at(b, s))) : 0.f;
+  const float ld = has_lo ? xlen(xsub3(lc, lo.at(b, l))) : 0.f;
+  const fv3 center = mkv(xmul(0.5f, xadd(sc.x, lc.x)), xmul(0.5f, xadd(sc.y, lc.y)),
+                         xmul(0.5f, xadd(sc.z, lc.z)));
+  fv3 nrm = xsub3(sc, lc);
+  const float length = xlen(nrm);
+  if (length > 1e-6f) {
+    const float inv = xdiv(1.f, length);
+    nrm = mkv(xmul(inv, nrm.x), xmul(inv, nrm.y), xmul(inv, nrm.z));
+  }
+  const fv3 rs = xsub3(mkv(xf, yf, g.sz), center);
+  const fv3 re = xsub3(mkv(xf, yf, g.ez), center);
+  const float* col = tr + (((size_t)b * T) * S + s) * L + l;
+  const size_t st = (size_t)S * L;
+  float* vb = vol + (size_t)b * g.D * g.H * g.W + c;
+  const size_t vs = (size_t)g.H * g.W;
+  for (int t = 0; t < T; ++t) {
+    const float value = __ldg(col + t * st);
+    if (!(value > 0.f)) continue;
+    const float tc = xsub(xsub(xadd(xmul((float)t, bw), bo), sd), ld);
+    if (!(tc > length)) continue;
+    const float r0 = xdiv(tc, 2.f);
+    const float r1 = xsqrt(xsub(xmul(r0, r0), xdiv(xmul(length, length), 4.f)));
+    const float scale = xdiv(r1, r0);
+    const float ks = xmul(xsub(scale, 1.f), xdot(rs, nrm));
+    const float ke = xmul(xsub(scale, 1.f), xdot(re, nrm));
+    const fv3 st0 = mkv(xfma(ks, nrm.x, rs.x), xfma(ks, nrm.y, rs.y), xfma(ks, nrm.z, rs.z));
+    const fv3 et = mkv(xfma(ke, nrm.x, re.x), xfma(ke, nrm.y, re.y), xfma(ke, nrm.z, re.z));
+    fv3 dir = xsub3(et, st0);
+    const float rl = xlen(dir);
+    const float ir = xdiv(1.f, rl);
+    dir = mkv(xmul(ir, dir.x), xmul(ir, dir.y), xmul(ir, dir.z));
+    const float v0 = xdot(dir, st0);
+    float v1 = xsub(xmul(v0, v0), xsub(xdot(st0, st0), xmul(r1, r1)));
+    if (!(v1 > 0.f)) continue;
+    v1 = xsqrt(v1);
+    float d = xsub(-v0, v1);
+    if (d < 0.f) d = xadd(-v0, v1);
+    const float bf = xadd(xmul(xdiv(d, rl), (float)g.D), 0.5f);
+    if (!(bf > -1.f && bf < (float)g.D)) continue;
+    atomicAdd(vb + (size_t)(int)bf * vs, value);
+  }
+}
+
+}  // namespace bp
+
+namespace {
+
+int check_volume_out(const totri_array_t* vol, bp::Grid& g, const float* start, const float* end,
+                     int64_t& B) {
+  TOTRI_TRY(check_array(vol, "volume", 4, -1));
+  if (vol->dtype != TOTRI_FLOAT32)
+    return fail(TOTRI_ERR_UNSUPPORTED, "backprojection: only float32 tensors are supported");
+  TOTRI_TRY(check_contiguous(vol, "volume"));
+  B = vol->shape[0];
+  g = bp::Grid{(int)vol->shape[1], (int)vol->shape[2], (int)vol->shape[3], start[0], start[1],
+               start[2], end[0], end[1], end[2]};
+  return TOTRI_OK;
+}
+
+int check_pts3(const totri_array_t* a, const char* name, int64_t B, int64_t& n, bp::Pts3& p) {
+  TOTRI_TRY(check_array(a, name, 3, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(a, name, 0, B));
+  TOTRI_TRY(check_dim(a, name, 2, 3));
+  n = a->shape[1];
+  p = bp::Pts3{static_cast<const float*>(a->data), a->strides[0], a->strides[1], a->strides[2]};
+  return TOTRI_OK;
+}
+
+int check_pts3t(const totri_array_t* a, const char* name, int64_t B, int64_t& n, bp::Pts3T& p) {
+  TOTRI_TRY(check_array(a, name, 3, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(a, name, 0, B));
+  TOTRI_TRY(check_dim(a, name, 1, 3));
+  n = a->shape[2];
+  p = bp::Pts3T{static_cast<const float*>(a->data), a->strides[0], a->strides[1], a->strides[2]};
+  return TOTRI_OK;
+}
+
+int origin_of(const totri_array_t* o, int64_t n, int has) {
+  (void)o;
+  (void)n;
+  return has;
+}
+
+}  // namespace
+}  // namespace totri
+
+using namespace totri;
+
+extern "C" {
+
+int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
+                                                 const totri_array_t* scan_points,
+                                                 const totri_array_t* scan_origin,
+                                                 const totri_array_t* volume, const float start[3],
+                                                 const float end[3], float bw, float bo,
+                                                 void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  bp::Grid g;
+  int64_t B, S, So;
+  TOTRI_TRY(check_volume_out(volume, g, start, end, B));
+  bp::Pts3 sp, so;
+  TOTRI_TRY(check_pts3(scan_points, "scan_points", B, S, sp));
+  TOTRI_TRY(check_pts3(scan_origin, "scan_origin", B, So, so));
+  if (So != 0 && So != S) return fail(TOTRI_ERR_INVALID_ARGUMENT, "scan_origin size mismatch");
+  TOTRI_TRY(check_array(transient, "transient", 3, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(transient, "transient", 0, B));
+  TOTRI_TRY(check_dim(transient, "transient", 2, S));
+  TOTRI_TRY(check_contiguous(transient, "transient"));
+  const int T = (int)transient->shape[1];
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  if (nv == 0 || B == 0) return TOTRI_OK;
+  for (int b = 0; b < (int)B; ++b)
+    TOTRI_KERNEL("backprojection velten confocal", stream,
+                 bp::velten_confocal_kernel<<<(unsigned)ceil_div(nv, 256), 256, 0, stream>>>(
+                     g, b, T, (int)S, sp, so, So > 0, bw, bo,
+                     static_cast<const float*>(transient->data),
+                     static_cast<float*>(volume->data)));
+  return TOTRI_OK;
+}
+
+int totri_backprojection_confocal_velten_adjoint(const totri_array_t* volume,
+                                                 const totri_array_t* scan_points,
+                                                 const totri_array_t* scan_origin,
+                                                 const totri_array_t* transient,
+                                                 const float start[3], const float end[3],
+                                                 float bw, float bo, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  bp::Grid g;
+  int64_t B, S, So;
+  TOTRI_TRY(check_volume_out(volume, g, start, end, B));
+  bp::Pts3 sp, so;
+  TOTRI_TRY(check_pts3(scan_points, "scan_points", B, S, sp));
+  TOTRI_TRY(check_pts3(scan_origin, "scan_origin", B, So, so));
+  if (So != 0 && So != S) return fail(TOTRI_ERR_INVALID_ARGUMENT, "scan_origin size mismatch");
+  TOTRI_TRY(check_array(transient, "transient", 3, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(transient, "transient", 0, B));
+  TOTRI_TRY(check_dim(transient, "transient", 2, S));
+  TOTRI_TRY(check_contiguous(transient, "transient"));
+  const int T = (int)transient->shape[1];
+  if (numel(transient) == 0) return TOTRI_OK;
+  const size_t smem = sizeof(float) * (size_t)T * bp::kTS;
+  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many bins for one tile");
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(bp::velten_adjoint_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = (int)smem;
+  }
+  for (int b = 0; b < (int)B; ++b)
+    TOTRI_KERNEL("backprojection velten adjoint", stream,
+                 bp::velten_adjoint_kernel<<<(unsigned)ceil_div(S, bp::kTS), 256, smem, stream>>>(
+                     g, b, T, (int)S, sp, so, So > 0, bw, bo,
+                     static_cast<const float*>(volume->data),
+                     static_cast<float*>(transient->data)));
+  return TOTRI_OK;
+}
+
+int totri_backprojection_exhaustive_velten_forward(
+    const totri_array_t* transient, const totri_array_t* scan_points,
+    const totri_array_t* laser_points, const totri_array_t* scan_origin,
+    const totri_array_t* laser_origin, const totri_array_t* volume, const float start[3],
+    const float end[3], float bw, float bo, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  bp::Grid g;
+  int64_t B, S, L, So, Lo;
+  TOTRI_TRY(check_volume_out(volume, g, start, end, B));
+  bp::Pts3 sp, lp, so, lo;
+  TOTRI_TRY(check_pts3(scan_points, "scan_points", B, S, sp));
+  TOTRI_TRY(check_pts3(laser_points, "laser_points", B, L, lp));
+  TOTRI_TRY(check_pts3(scan_origin, "scan_origin", B, So, so));
+  TOTRI_TRY(check_pts3(laser_origin, "laser_origin", B, Lo, lo));
+  if ((So != 0 && So != S) || (Lo != 0 && Lo != L))
+    return fail(TOTRI_ERR_INVALID_ARGUMENT, "origin size mismatch");
+  TOTRI_TRY(check_array(transient, "transient", 4, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(transient, "transient", 0, B));
+  TOTRI_TRY(check_dim(transient, "transient", 2, S));
+  TOTRI_TRY(check_dim(transient, "transient", 3, L));
+  TOTRI_TRY(check_contiguous(transient, "transient"));
+  const int T = (int)transient->shape[1];
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  if (nv == 0) return TOTRI_OK;
+  for (int b = 0; b < (int)B; ++b)
+    TOTRI_KERNEL("backprojection velten exhaustive", stream,
+                 bp::velten_exhaustive_kernel<<<(unsigned)ceil_div(nv, 128), 128, 0, stream>>>(
+                     g, b, T, (int)S, (int)L, sp, lp, so, lo, So > 0, Lo > 0, bw, bo,
+                     static_cast<const float*>(transient->data),
+                     static_cast<float*>(volume->data)));
+  return TOTRI_OK;
+}
+
+int totri_backprojection_exhaustive_arellano_forward(
+    const totri_array_t* transient, const totri_array_t* scan_points,
+    const totri_array_t* laser_points, const totri_array_t* scan_origin,
+    const totri_array_t* laser_origin, const totri_array_t* volume, const float start[3],
+    const float end[3], float bw, float bo, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  bp::Grid g;
+  int64_t B, S, L, So, Lo;
+  TOTRI_TRY(check_volume_out(volume, g, start, end, B));
+  bp::Pts3T sp, lp, so, lo;
+  TOTRI_TRY(check_pts3t(scan_points, "scan_points", B, S, sp));
+  TOTRI_TRY(check_pts3t(laser_points, "laser_points", B, L, lp));
+  TOTRI_TRY(check_pts3t(scan_origin, "scan_origin", B, So, so));
+  TOTRI_TRY(check_pts3t(laser_origin, "laser_origin", B, Lo, lo));
+  if ((So != 0 && So != S) || (Lo != 0 && Lo != L))
+    return fail(TOTRI_ERR_INVALID_ARGUMENT, "origin size mismatch");
+  TOTRI_TRY(check_array(transient, "transient", 4, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(transient, "transient", 0, B));
+  TOTRI_TRY(check_dim(transient, "transient", 2, S));
+  TOTRI_TRY(check_dim(transient, "transient", 3, L));
+  TOTRI_TRY(check_contiguous(transient, "transient"));
+  const int T = (int)transient->shape[1];
+  if (g.H * g.W == 0 || S == 0 || L == 0) return TOTRI_OK;
+  for (int b = 0; b < (int)B; ++b) {
+    const dim3 grid((unsigned)ceil_div(g.H * g.W, 64), (unsigned)S, (unsigned)L);
+    TOTRI_KERNEL("backprojection arellano", stream,
+                 bp::arellano_kernel<<<grid, 64, 0, stream>>>(
+                     g, b, T, (int)S, (int)L, sp, lp, so, lo, origin_of(scan_origin, S, So > 0),
+                     origin_of(laser_origin, L, Lo > 0), bw, bo,
+                     static_cast<const float*>(transient->data),
+                     static_cast<float*>(volume->data)));
+  }
+  return TOTRI_OK;
+}
+
+}  // extern "C"

@@ -171,6 +171,67 @@ int confocal_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
                                     (int)S, bin_width, bin_offset, out, stream);
 }
 
+struct ExhArgs {
+  MeshArgs m;
+  int64_t S, L, T;
+  mesh::Origins org;
+};
+
+int check_exhaustive(const totri_array_t* verts, const totri_array_t* faces,
+                     const totri_array_t* material, const totri_array_t* scan_points,
+                     const totri_array_t* laser_points, const totri_array_t* scan_origin,
+                     const totri_array_t* laser_origin, const totri_array_t* tr, const char* tname,
+                     ExhArgs& e) {
+  TOTRI_TRY(check_mesh(verts, faces, material, e.m));
+  TOTRI_TRY(check_points(scan_points, "scan_points", e.m.B, e.S));
+  TOTRI_TRY(check_points(laser_points, "laser_points", e.m.B, e.L));
+  TOTRI_TRY(check_origin(scan_origin, "scan_origin", e.m.B, e.S, e.org.has_so));
+  TOTRI_TRY(check_origin(laser_origin, "laser_origin", e.m.B, e.L, e.org.has_lo));
+  e.org.so = view3f(scan_origin);
+  e.org.lo = view3f(laser_origin);
+  TOTRI_TRY(check_array(tr, tname, 4, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(tr, tname, 0, e.m.B));
+  TOTRI_TRY(check_dim(tr, tname, 2, e.S));
+  TOTRI_TRY(check_dim(tr, tname, 3, e.L));
+  TOTRI_TRY(check_contiguous(tr, tname));
+  e.T = tr->shape[1];
+  if (e.S + e.L >= (int64_t)1 << 30 || e.T >= (int64_t)1 << 30)
+    return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points or bins");
+  return TOTRI_OK;
+}
+
+int exhaustive_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
+                         const totri_array_t* material, const totri_array_t* scan_points,
+                         const totri_array_t* laser_points, const totri_array_t* scan_origin,
+                         const totri_array_t* laser_origin, const totri_array_t* transient_grad,
+                         const totri_array_t* verts_grad, const totri_array_t* material_grad,
+                         float bw, float bo, void* ws, size_t ws_bytes, void* stream_,
+                         bool reuse) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  ExhArgs e;
+  TOTRI_TRY(check_exhaustive(verts, faces, material, scan_points, laser_points, scan_origin,
+                             laser_origin, transient_grad, "transient_grad", e));
+  mesh::GradOut out;
+  TOTRI_TRY(check_grads(verts_grad, material_grad, e.m, out));
+  TOTRI_TRY(zero3(verts_grad, stream));
+  TOTRI_TRY(zero3(material_grad, stream));
+  if (e.m.F == 0 || e.S == 0 || e.L == 0 || e.T == 0 || e.m.B == 0 || (!out.vg && !out.mg))
+    return TOTRI_OK;
+  const int64_t P = e.S + e.L;
+  TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(e.m.B, e.m.F, P).total));
+  const mesh::Scene sc = mesh::scene_from_workspace(ws, e.m.B, e.m.F, P);
+  if (!reuse) {
+    TOTRI_TRY(mesh::build_scene(sc, e.m.in, stream));
+    TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)e.S, 0, false, stream));
+    TOTRI_TRY(
+        mesh::launch_visibility(sc, view3f(laser_points), (int)e.L, (int)e.S, false, stream));
+  }
+  return mesh::launch_exhaustive_grad(sc, view3f(scan_points), view3f(laser_points), e.org,
+                                      (int)e.S, (int)e.L,
+                                      static_cast<const float*>(transient_grad->data), (int)e.T,
+                                      bw, bo, out, stream);
+}
+
 }  // namespace
 }  // namespace totri
 
@@ -254,6 +315,64 @@ int totri_mesh_confocal_grad_verts_reuse(const totri_array_t* verts, const totri
   return confocal_grad_impl(verts, faces, material, scan_points, scan_origin, transient_grad,
                             verts_grad, material_grad, bin_width, bin_offset, ws, ws_bytes,
                             stream, true);
+}
+
+int totri_mesh_exhaustive_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                  const totri_array_t* material,
+                                  const totri_array_t* scan_points,
+                                  const totri_array_t* laser_points,
+                                  const totri_array_t* scan_origin,
+                                  const totri_array_t* laser_origin,
+                                  const totri_array_t* transient, float bw, float bo, int model,
+                                  void* ws, size_t ws_bytes, void* stream_) {
+  (void)model;
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  ExhArgs e;
+  TOTRI_TRY(check_exhaustive(verts, faces, material, scan_points, laser_points, scan_origin,
+                             laser_origin, transient, "transient", e));
+  if (numel(transient) == 0) return TOTRI_OK;
+  if (e.m.F == 0) {
+    TOTRI_CUDA(cudaMemsetAsync(transient->data, 0, sizeof(float) * numel(transient), stream));
+    return TOTRI_OK;
+  }
+  const int64_t P = e.S + e.L;
+  TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(e.m.B, e.m.F, P).total));
+  const mesh::Scene sc = mesh::scene_from_workspace(ws, e.m.B, e.m.F, P);
+  TOTRI_TRY(mesh::build_scene(sc, e.m.in, stream));
+  TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)e.S, 0, false, stream));
+  TOTRI_TRY(mesh::launch_visibility(sc, view3f(laser_points), (int)e.L, (int)e.S, false, stream));
+  return mesh::launch_exhaustive_splat(sc, view3f(scan_points), view3f(laser_points), e.org,
+                                       (int)e.S, (int)e.L, static_cast<float*>(transient->data),
+                                       (int)e.T, bw, bo, stream);
+}
+
+int totri_mesh_exhaustive_grad_verts(const totri_array_t* verts, const totri_array_t* faces,
+                                     const totri_array_t* material,
+                                     const totri_array_t* scan_points,
+                                     const totri_array_t* laser_points,
+                                     const totri_array_t* scan_origin,
+                                     const totri_array_t* laser_origin,
+                                     const totri_array_t* transient_grad,
+                                     const totri_array_t* verts_grad,
+                                     const totri_array_t* material_grad, float bw, float bo,
+                                     int model, void* ws, size_t ws_bytes, void* stream) {
+  (void)model;
+  return exhaustive_grad_impl(verts, faces, material, scan_points, laser_points, scan_origin,
+                              laser_origin, transient_grad, verts_grad, material_grad, bw, bo, ws,
+                              ws_bytes, stream, false);
+}
+
+int totri_mesh_exhaustive_grad_verts_reuse(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* laser_points,
+    const totri_array_t* scan_origin, const totri_array_t* laser_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bw, float bo, int model, void* ws, size_t ws_bytes,
+    void* stream) {
+  (void)model;
+  return exhaustive_grad_impl(verts, faces, material, scan_points, laser_points, scan_origin,
+                              laser_origin, transient_grad, verts_grad, material_grad, bw, bo, ws,
+                              ws_bytes, stream, true);
 }
 
 int totri_mesh_visibility(const totri_array_t* verts, const totri_array_t* faces,

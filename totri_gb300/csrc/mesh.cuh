@@ -282,5 +282,88 @@ __device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, 
   return true;
 }
 
+// One ray of the persistent visibility walk, advanced one BVH node per step.
+struct RayState {
+  fv3 o, dir, inv, oinv;
+  float tf, tmax;
+  int k, f;
+  int node, sp;
+  int it;
+};
+
+// Sets up the ray from o to the centroid of face k. Returns 0 when the ray is
+// decided without a walk (not visible), 1 when the face is visible with no
+// walk needed (a single face), 2 when the walk must run.
+__device__ __forceinline__ int ray_setup(const Scene& sc, int b, int n, int k, fv3 o,
+                                         RayState& r) {
+  const Target tg = load_target(sc, b, k);
+  const fv3 D = xsub3(tg.c, o);
+  const float dist = xlen(D);
+  if (!(dist >= 1e-6f)) return 0;
+  r.o = o;
+  r.dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+  r.tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+  r.k = k;
+  r.f = tg.f;
+  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, r.dir, r.tmax, r.tf)) return 0;
+  if (n == 1) return 1;
+  r.inv = mkv(safe_inv(r.dir.x), safe_inv(r.dir.y), safe_inv(r.dir.z));
+  r.oinv = mkv(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+  r.node = 0;
+  r.sp = 0;
+  r.it = 0;
+  return 2;
+}
+
+// One node of the walk. Returns 0 (occluded), 1 (stack empty: visible) or
+// 2 (continue). Same decisions as target_visible.
+__device__ __forceinline__ int ray_step(const Scene& sc, int b, int n, RayState& r, int* stack,
+                                        uint32_t* status) {
+  auto occludes = [&](int kk) -> bool {
+    if (kk == r.k) return false;
+    if (kk < 0 || kk >= n) {
+      atomicOr(status, kStatusTraversalCap);
+      return false;
+    }
+    const float4* q = tri_at(sc, b, kk);
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+    float tq;
+    if (!tri_hit(q0, q1, q2, q3, r.o, r.dir, r.tmax, tq)) return false;
+    return tq < r.tf || (tq == r.tf && __float_as_int(q3.w) < r.f);
+  };
+  if (r.node < 0 || r.node >= n - 1 || ++r.it > 2 * n + 64) {
+    atomicOr(status, kStatusTraversalCap);
+    return 1;
+  }
+  const float4* nd = node_at(sc, b, r.node);
+  const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+  float tn0, tn1;
+  bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, r.inv, r.oinv, r.tf, tn0);
+  bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, r.inv, r.oinv, r.tf, tn1);
+  const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+  if (h0 && c0 < 0) {
+    if (occludes(~c0)) return 0;
+    h0 = false;
+  }
+  if (h1 && c1 < 0) {
+    if (occludes(~c1)) return 0;
+    h1 = false;
+  }
+  if (h0 && h1) {
+    const bool first0 = tn0 <= tn1;
+    if (r.sp < 64) stack[r.sp++] = first0 ? c1 : c0;
+    else atomicOr(status, kStatusTraversalCap);
+    r.node = first0 ? c0 : c1;
+  } else if (h0) {
+    r.node = c0;
+  } else if (h1) {
+    r.node = c1;
+  } else {
+    if (r.sp == 0) return 1;
+    r.node = stack[--r.sp];
+  }
+  return 2;
+}
+
 }  // namespace mesh
 }  // namespace totri

@@ -214,6 +214,83 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
   }
 }
 
+// Persistent BVH walk: each warp owns kVisUnits mask words (32 rays each, in
+// (batch, point, face chunk) order, so consecutive rays share an origin and
+// end on neighbouring faces). A lane whose ray finishes takes the next ray of
+// the warp's pool; the warp keeps stepping while at least kVisRefill lanes are
+// busy, then refills idle lanes together (rays decided at set-up free their
+// lane at once). Visible rays set their bit in a shared word per unit.
+constexpr int kVisUnits = 16;
+constexpr int kVisWarps = 8;
+constexpr int kVisRefill = 20;
+
+__global__ void __launch_bounds__(256) visibility_walk_kernel(Scene sc, View3f pts, int P,
+                                                              int row0) {
+  __shared__ uint32_t words[kVisWarps][kVisUnits];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t per_b = (int64_t)P * sc.nch;
+  const int64_t total_units = per_b * sc.B;
+  const int64_t u0 = ((int64_t)blockIdx.x * kVisWarps + warp) * kVisUnits;
+  if (u0 >= total_units) return;  // whole warp
+  if (lane < kVisUnits) words[warp][lane] = 0;
+  __syncwarp();
+  const int nrays = (int)min((int64_t)kVisUnits, total_units - u0) * 32;
+  const uint32_t lt = (1u << lane) - 1u;
+  int next = 0;  // warp-uniform
+  bool busy = false;
+  int ray = 0, b = 0, n = 0;
+  RayState r;
+  int stack[64];
+  while (true) {
+    // refill idle lanes; a ray decided at set-up leaves its lane idle for the next round
+    while (next < nrays) {
+      const bool idle = !busy;
+      const uint32_t im = __ballot_sync(0xffffffffu, idle);
+      if (im == 0) break;
+      const int mine = next + __popc(im & lt);
+      next += __popc(im);
+      if (idle && mine < nrays) {
+        ray = mine;
+        const int64_t G = u0 + (ray >> 5);
+        b = (int)(G / per_b);
+        const int64_t rem = G - (int64_t)b * per_b;
+        const int p = (int)(rem / sc.nch);
+        const int ch = (int)(rem - (int64_t)p * sc.nch);
+        n = sc.meta[b].n;
+        const int k = ch * 32 + (ray & 31);
+        if (k < n) {
+          const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
+          const int st = ray_setup(sc, b, n, k, o, r);
+          if (st == 2) busy = true;
+          else if (st == 1) atomicOr(&words[warp][ray >> 5], 1u << (ray & 31));
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, busy) == 0) break;
+    // walk while enough lanes are busy (or until all are done once the pool is empty)
+    while (true) {
+      if (busy) {
+        const int st = ray_step(sc, b, n, r, stack, sc.status);
+        if (st != 2) {
+          busy = false;
+          if (st == 1) atomicOr(&words[warp][ray >> 5], 1u << (ray & 31));
+        }
+      }
+      const int nb = __popc(__ballot_sync(0xffffffffu, busy));
+      if (nb == 0 || (next < nrays && nb < kVisRefill)) break;
+    }
+  }
+  __syncwarp();
+  if (lane < kVisUnits && u0 + lane < total_units) {
+    const int64_t G = u0 + lane;
+    const int bb = (int)(G / per_b);
+    const int64_t rem = G - (int64_t)bb * per_b;
+    const int p = (int)(rem / sc.nch);
+    const int ch = (int)(rem - (int64_t)p * sc.nch);
+    sc.mask[((size_t)bb * sc.P + row0 + p) * sc.nch + ch] = words[warp][lane];
+  }
+}
+
 // Re-indexes mask bits from Morton order (bit k) to input face order (bit f).
 __global__ void mask_unsort_kernel(Scene sc, int P, uint32_t* out) {
   const int b = blockIdx.y;
@@ -238,15 +315,18 @@ int launch_mask_unsort(const Scene& sc, int P, uint32_t* out, cudaStream_t strea
 
 int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool brute,
                       cudaStream_t stream) {
-  const int64_t warps = (int64_t)sc.B * P * sc.nch;
-  if (warps == 0) return TOTRI_OK;
-  const int64_t blocks = ceil_div(warps * 32, 256);
-  if (brute)
+  const int64_t units = (int64_t)sc.B * P * sc.nch;
+  if (units == 0) return TOTRI_OK;
+  if (brute) {
+    const int64_t blocks = ceil_div(units * 32, 256);
     TOTRI_KERNEL("mesh visibility brute", stream,
                  visibility_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(sc, pts, P, row0));
-  else
+  } else {
+    const int64_t blocks = ceil_div(units, (int64_t)kVisUnits * kVisWarps);
     TOTRI_KERNEL("mesh visibility", stream,
-                 visibility_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(sc, pts, P, row0));
+                 visibility_walk_kernel<<<(unsigned)blocks, 32 * kVisWarps, 0, stream>>>(
+                     sc, pts, P, row0));
+  }
   return TOTRI_OK;
 }
 

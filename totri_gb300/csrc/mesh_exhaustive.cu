@@ -1,0 +1,265 @@
+// Exhaustive (separate laser and detector points) mesh transient rendering:
+// forward splat and vertex / albedo gradient.
+//
+// Reference: src/render/program/mesh_exhaustive_forward_optix.cu:18-169 and
+// mesh_exhaustive_grad_verts_optix.cu:18-248: one OptiX thread per (face,
+// scan, laser) triple tracing two visibility rays, global atomics into
+// transient[b][bin][s][l]. Here visibility is separable: face f is visible
+// from scan point s and from laser point l independently, so the two masks
+// are computed once (S + L rows of the shared mask buffer) and each triple is
+// their AND. The forward gives each CTA one scan point and a tile of laser
+// points with a [T][tile] shared histogram flushed as rows of the [T][S][L]
+// output; the gradient gives each CTA 32 faces and walks every (s, l) pair.
+#include "capi_common.cuh"
+#include "mesh.cuh"
+#include "mesh_kernels.cuh"
+
+namespace totri {
+namespace mesh {
+
+struct ExhPair {
+  fv3 v[3];
+  int perm[3];
+  float d[3];   // scan + laser path length (sort key)
+  float ds[3];  // vertex - scan distance
+  float dl[3];  // vertex - laser distance
+  float c[3];
+  int bin[3];
+};
+
+__device__ __forceinline__ void exh_sort(ExhPair& q) {
+  auto sw = [&](int i, int j) {
+    float t = q.d[i]; q.d[i] = q.d[j]; q.d[j] = t;
+    t = q.ds[i]; q.ds[i] = q.ds[j]; q.ds[j] = t;
+    t = q.dl[i]; q.dl[i] = q.dl[j]; q.dl[j] = t;
+    fv3 tv = q.v[i]; q.v[i] = q.v[j]; q.v[j] = tv;
+    int tp = q.perm[i]; q.perm[i] = q.perm[j]; q.perm[j] = tp;
+  };
+  if (q.d[0] > q.d[1]) sw(0, 1);
+  if (q.d[1] > q.d[2]) sw(1, 2);
+  if (q.d[0] > q.d[1]) sw(0, 1);
+}
+
+// FP32 decisions exactly as the oracle takes them (exhaustive_geom).
+__device__ __forceinline__ void exh_pair(float4 s0, float4 s1, float4 s2, fv3 sp, fv3 lp, float od,
+                                         float bw, float bo, ExhPair& q) {
+  q.v[0] = mkv(s0.x, s0.y, s0.z);
+  q.v[1] = mkv(s1.x, s1.y, s1.z);
+  q.v[2] = mkv(s2.x, s2.y, s2.z);
+  for (int k = 0; k < 3; ++k) {
+    q.perm[k] = k;
+    q.ds[k] = xlen(xsub3(q.v[k], sp));
+    q.dl[k] = xlen(xsub3(q.v[k], lp));
+    q.d[k] = xadd(q.ds[k], q.dl[k]);
+  }
+  exh_sort(q);
+  for (int k = 0; k < 3; ++k) {
+    q.c[k] = xdiv(xsub(xadd(q.d[k], od), bo), bw);
+    q.bin[k] = bin_of(q.c[k]);
+  }
+}
+
+// AlphaExhaustive (mesh_common.h:505-531), wall normals (0,0,1).
+__device__ __forceinline__ float alpha_exhaustive(const ExhPair& q, fv3 c, fv3 sp, fv3 lp,
+                                                  float rho) {
+  const fv3 n = cross(q.v[1] - q.v[0], q.v[2] - q.v[0]);
+  const fv3 rs = c - sp, rl = c - lp;
+  if (!(rs.z > 0.f) || !(rl.z > 0.f)) return 0.f;
+  const float rss = dot(rs, rs), rll = dot(rl, rl);
+  return 100.f * rho * rs.z * rl.z * fabsf(dot(n, rs)) * fabsf(dot(n, rl)) /
+         (sqrtf(dot(n, n)) * (rss * rss) * (rll * rll));
+}
+
+__device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int l, fv3 sp,
+                                             fv3 lp) {
+  float od = 0.f;
+  if (o.has_so) od = xlen(xsub3(sp, mkv(o.so.at(b, s, 0), o.so.at(b, s, 1), o.so.at(b, s, 2))));
+  if (o.has_lo)
+    od = xadd(od, xlen(xsub3(lp, mkv(o.lo.at(b, l, 0), o.lo.at(b, l, 1), o.lo.at(b, l, 2)))));
+  return od;
+}
+
+template <int LT>
+__global__ void __launch_bounds__(256) exh_splat_kernel(Scene sc, View3f sp, View3f lp, Origins org,
+                                                        int S, int L, float* __restrict__ out,
+                                                        int T, float bw, float bo) {
+  extern __shared__ float hist[];  // [T][LT]
+  const int b = blockIdx.z;
+  const int s = blockIdx.x;
+  const int l0 = blockIdx.y * LT;
+  for (int i = threadIdx.x; i < T * LT; i += blockDim.x) hist[i] = 0.f;
+  __syncthreads();
+  const int n = sc.meta[b].n;
+  const int ll = threadIdx.x % LT;
+  const int l = l0 + ll;
+  if (l < L) {
+    const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+    const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
+    const float od = origin_term(org, b, s, l, p, q);
+    const uint32_t* ms = sc.mask + ((size_t)b * sc.P + s) * sc.nch;
+    const uint32_t* ml = sc.mask + ((size_t)b * sc.P + S + l) * sc.nch;
+    const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+    Hist<LT> h{hist, ll, T};
+    for (int k = threadIdx.x / LT; k < n; k += blockDim.x / LT) {
+      const uint32_t bit = 1u << (k & 31);
+      if (!(__ldg(ms + (k >> 5)) & bit) || !(__ldg(ml + (k >> 5)) & bit)) continue;
+      const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+      const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+      ExhPair e;
+      exh_pair(s0r, s1r, s2r, p, q, od, bw, bo, e);
+      const float alpha = alpha_exhaustive(e, mkv(s3r.x, s3r.y, s3r.z), p, q, s0r.w);
+      if (!(alpha > 0.f)) continue;
+      splat_tent(h, e.c, e.bin, alpha);
+    }
+  }
+  __syncthreads();
+  // rows out[b][t][s][l0 .. l0+LT)
+  float* ob = out + (((size_t)b * T) * S + s) * L + l0;
+  for (int i = threadIdx.x; i < T * LT; i += blockDim.x) {
+    const int t = i / LT, c = i - t * LT;
+    if (l0 + c < L) ob[(size_t)t * S * L + c] = hist[i];
+  }
+}
+
+// Gradient of one visible triple w.r.t. the sorted vertices and the albedo
+// (mesh_exhaustive_grad_verts_optix.cu:336-412, AlphaExhaustiveGradVerts
+// mesh_common.h:549-630).
+__device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3 lp, float rho,
+                                            float bw, const float* __restrict__ col,
+                                            int64_t stride, int T, fv3 dv[3], float& dmat) {
+  const float alpha = alpha_exhaustive(q, c, sp, lp, rho);
+  if (!(alpha > 0.f)) return false;
+  if (q.bin[0] >= T || q.bin[2] < 0) return false;
+  const fv3 e1 = q.v[1] - q.v[0], e2 = q.v[2] - q.v[0];
+  const fv3 n = cross(e1, e2);
+  const fv3 rs = c - sp, rl = c - lp;
+  const float kn = -1.f / dot(n, n);
+  const float krs = -4.f / (3.f * dot(rs, rs)), krl = -4.f / (3.f * dot(rl, rl));
+  const float kw = 1.f / (3.f * rs.z) + 1.f / (3.f * rl.z);
+  const float knrs = 1.f / dot(n, rs), knrl = 1.f / dot(n, rl);
+  const fv3 w = kn * n + knrs * rs + knrl * rl;
+  const fv3 g1 = cross(e2, w), g2 = cross(w, e1);
+  const fv3 common = krs * rs + krl * rl + ((knrs + knrl) * (1.f / 3.f)) * n + mkv(0.f, 0.f, kw);
+  const fv3 da0 = alpha * (common - g1 - g2);
+  const fv3 da1 = alpha * (common + g1);
+  const fv3 da2 = alpha * (common + g2);
+  const float dadm = alpha / rho;
+  if (q.bin[0] == q.bin[2]) {
+    const float g = __ldg(col + (size_t)q.bin[0] * stride);
+    dv[0] = g * da0;
+    dv[1] = g * da1;
+    dv[2] = g * da2;
+    dmat = g * dadm;
+    return true;
+  }
+  TentGrad tgr;
+  tent_grad(col, stride, T, q.c, q.bin, tgr);
+  const float span = q.c[2] - q.c[0];
+  const float kk = -2.f / (bw * span * span);
+  fv3 dc[3];
+  for (int k = 0; k < 3; ++k)
+    dc[k] = (1.f / (bw * q.dl[k])) * (q.v[k] - lp) + (1.f / (bw * q.ds[k])) * (q.v[k] - sp);
+  const fv3 dyc0 = kk * ((1.f / -q.dl[0]) * (q.v[0] - lp) + (1.f / -q.ds[0]) * (q.v[0] - sp));
+  const fv3 dyc2 = kk * ((1.f / q.dl[2]) * (q.v[2] - lp) + (1.f / q.ds[2]) * (q.v[2] - sp));
+  dv[0] = tgr.part0 * da0 + alpha * (tgr.ayc * dyc0 + tgr.a0 * dc[0]);
+  dv[1] = tgr.part0 * da1 + alpha * (tgr.a1 * dc[1]);
+  dv[2] = tgr.part0 * da2 + alpha * (tgr.ayc * dyc2 + tgr.a2 * dc[2]);
+  dmat = dadm * tgr.part0;
+  return true;
+}
+
+__global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View3f lp, Origins org,
+                                                       int S, int L,
+                                                       const float* __restrict__ tgrad, int T,
+                                                       float bw, float bo, GradOut out) {
+  extern __shared__ uint32_t mcol[];  // [S + L] mask words of this 32-face chunk
+  const int b = blockIdx.y;
+  const int ch = blockIdx.x;
+  const int n = sc.meta[b].n;
+  if (ch * 32 >= n) return;
+  for (int i = threadIdx.x; i < S + L; i += blockDim.x)
+    mcol[i] = sc.mask[((size_t)b * sc.P + i) * sc.nch + ch];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const float* tgb = tgrad + (size_t)b * T * S * L;
+  const int64_t stride = (int64_t)S * L;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  for (int j = warp; j < 32; j += nw) {
+    const int k = ch * 32 + j;
+    if (k >= n) break;
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
+    fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
+    float accm = 0.f;
+    for (int s = 0; s < S; ++s) {
+      if (!((mcol[s] >> j) & 1u)) continue;
+      const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+      for (int l = lane; l < L; l += 32) {
+        if (!((mcol[S + l] >> j) & 1u)) continue;
+        const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
+        ExhPair e;
+        exh_pair(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, e);
+        fv3 dv[3];
+        float dm;
+        if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
+          continue;
+        for (int kk = 0; kk < 3; ++kk) acc[e.perm[kk]] = acc[e.perm[kk]] + dv[kk];
+        accm += dm;
+      }
+    }
+    scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
+  }
+}
+
+template <int LT>
+static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
+                            const Origins& org, int S, int L, float* out, int T, float bw,
+                            float bo, cudaStream_t stream) {
+  const size_t smem = sizeof(float) * (size_t)T * LT;
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = (int)smem;
+  }
+  const dim3 grid((unsigned)S, (unsigned)ceil_div(L, LT), (unsigned)sc.B);
+  TOTRI_KERNEL("mesh exhaustive splat", stream,
+               exh_splat_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, out, T, bw,
+                                                                 bo));
+  return TOTRI_OK;
+}
+
+int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
+                            const Origins& org, int S, int L, float* out, int T, float bw,
+                            float bo, cudaStream_t stream) {
+  const size_t budget = 200 * 1024;
+  if ((size_t)T * 16 * 4 <= budget && L >= 16)
+    return launch_exh_splat<16>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+  if ((size_t)T * 4 * 4 <= budget && L >= 4)
+    return launch_exh_splat<4>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+  if ((size_t)T * 4 <= budget)
+    return launch_exh_splat<1>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+  return fail(TOTRI_ERR_UNSUPPORTED, "number of bins too large for the shared-memory tile");
+}
+
+int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
+                           const Origins& org, int S, int L, const float* tgrad, int T, float bw,
+                           float bo, const GradOut& out, cudaStream_t stream) {
+  const size_t smem = sizeof(uint32_t) * (size_t)(S + L);
+  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points for one tile");
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    configured = (int)smem;
+  }
+  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B);
+  TOTRI_KERNEL("mesh exhaustive grad", stream,
+               exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T, bw,
+                                                            bo, out));
+  return TOTRI_OK;
+}
+
+}  // namespace mesh
+}  // namespace totri

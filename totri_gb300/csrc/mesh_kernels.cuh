@@ -217,6 +217,19 @@ __device__ __forceinline__ void scatter_face_grad(const GradOut& out, int b, flo
 // Host launchers.
 int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool brute,
                       cudaStream_t stream);
+// Wall-to-origin terms of the exhaustive renderer (detector and laser).
+struct Origins {
+  View3f so, lo;
+  int has_so, has_lo;
+};
+
+int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
+                            const Origins& org, int S, int L, float* out, int T, float bw,
+                            float bo, cudaStream_t stream);
+int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
+                           const Origins& org, int S, int L, const float* tgrad, int T, float bw,
+                           float bo, const GradOut& out, cudaStream_t stream);
+
 int launch_mask_unsort(const Scene& sc, int P, uint32_t* out, cudaStream_t stream);
 int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
                           float* transient, int T, int S, float bw, float bo, cudaStream_t stream);

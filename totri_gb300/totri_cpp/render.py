@@ -67,10 +67,17 @@ def mesh_exhaustive_grad_verts(verts, faces, material, scan_points, laser_points
                bin_width, bin_offset, model, scan_points.shape[1] + laser_points.shape[1])
 
 
-def _vol_call(name, tensors, a3, b3, bw, bo, device):
+def _vol_call(name, tensors, a3, b3, bw, bo, device, voxels=None):
+    """Calls a volume entry point; `voxels` (voxels per batch item) adds the
+    occupied-voxel scratch those entry points need."""
     lib = _lib.load()
+    extra = ()
+    if voxels is not None:
+        n = int(lib.totri_volume_workspace(int(voxels)))
+        ws = torch.empty(max(n, 1), dtype=torch.uint8, device=device)
+        extra = ws_args(ws)
     st = getattr(lib, name)(*[_lib.array(t) for t in tensors], _lib.vec3(a3), _lib.vec3(b3),
-                            float(bw), float(bo), _lib.stream_of(device))
+                            float(bw), float(bo), *extra, _lib.stream_of(device))
     _lib.check(st)
 
 
@@ -82,7 +89,7 @@ def volume_confocal_forward(volume, measurement_points, transient, volume_origin
         raise ValueError("Measurement and transient dimensions do not match.")
     out = dense_out(transient)
     _vol_call("totri_volume_confocal_forward", (volume.contiguous(), measurement_points, out),
-              volume_origin, volume_size, bin_width, bin_offset, volume.device)
+              volume_origin, volume_size, bin_width, bin_offset, volume.device, volume.numel())
     finish_out(transient, out)
 
 
@@ -119,7 +126,7 @@ def volume_confocal_grad_measurement_points(measurement_points_grad, volume,
     out = dense_out(measurement_points_grad)
     _vol_call("totri_volume_confocal_grad_measurement_points",
               (out, volume.contiguous(), measurement_points, transient_grad.contiguous()),
-              volume_origin, volume_size, bin_width, bin_offset, volume.device)
+              volume_origin, volume_size, bin_width, bin_offset, volume.device, volume.numel())
     finish_out(measurement_points_grad, out)
 
 
@@ -131,7 +138,8 @@ def volume_render_exhaustive_forward(volume, scan_points, laser_points, scan_ori
     out = dense_out(transient)
     _vol_call("totri_volume_exhaustive_forward",
               (volume.contiguous(), scan_points, laser_points, scan_origin, laser_origin, out),
-              volume_start, volume_end, bin_width, bin_offset, volume.device)
+              volume_start, volume_end, bin_width, bin_offset, volume.device,
+              volume[0].numel() if volume.shape[0] > 0 else 0)
     finish_out(transient, out)
 
 
