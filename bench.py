@@ -52,6 +52,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-secondary", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-serve", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=None)
     return p.parse_args()
 
@@ -182,6 +185,247 @@ def mean_segments(w, device, stride=8):
     return float(seg.mean())
 
 
+def _timed(fn, flush, reps, warmup=3):
+    """Mean device milliseconds of fn() over reps calls (L2 flushed between calls)."""
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    total = 0.0
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / reps
+
+
+def secondary_metrics(device, flush, reps=5):
+    """The other throughputs named by the headline metric, on the 128^3 workloads:
+    Velten backprojection (128^3 voxels x 128x128 scan points x 1024 bins),
+    volume render + exact adjoint, and RBF splat + gradient (4096 Gaussians)."""
+    from totri_gb300 import scenes
+    from totri_gb300.totri_cpp import reconstruct as K
+    from totri_gb300.totri_cpp import render as R
+    from totri_gb300.totri_cpp import util as U
+    s = scenes.volume_scene()
+    vd, bd = s["volume_def"], s["bin_def"]
+    sp = s["scan_points"].to(device)
+    S = sp.shape[1]
+    nvox = int(np.prod(vd.resolution))
+    tr = torch.rand((1, bd.num, S), device=device)
+    vol_out = torch.empty((1,) + tuple(vd.resolution), device=device)
+    empty = torch.empty_like(sp[:, :0])
+    ms_bp = _timed(lambda: K.backprojection_confocal_velten_forward(
+        tr, sp, empty, vol_out, vd.start, vd.end, bd.width, bd.offset), flush, reps)
+    vol = s["volume"].to(device)
+    mp = sp[0].T.contiguous()
+    size = tuple(e - a for a, e in zip(vd.start, vd.end))
+    trv = torch.empty((S, bd.num), device=device)
+    adj = torch.empty_like(vol)
+    ms_vf = _timed(lambda: R.volume_confocal_forward(vol, mp, trv, vd.start, size, bd.width,
+                                                     bd.offset), flush, reps)
+    ms_va = _timed(lambda: R.volume_confocal_adjoint(adj, mp, trv, vd.start, size, bd.width,
+                                                     bd.offset), flush, 2)
+    rbf = scenes.rbf_set(4096, seed=5).to(device)
+    rvol = torch.empty((1, 2) + tuple(vd.resolution), device=device)
+    ms_rf = _timed(lambda: U.rbf2volume_gaussian_forward(rbf, rvol, vd.start, vd.end), flush,
+                   reps)
+    rgrad = torch.zeros_like(rbf)
+    vg = torch.randn_like(rvol)
+    ms_rg = _timed(lambda: U.rbf2volume_gaussian_grad(rbf, rvol, vg, rgrad, vd.start, vd.end),
+                   flush, reps)
+    pairs = nvox * S
+    return {
+        "backproj voxel·scanpt/s": {"value": pairs / (ms_bp / 1e3), "ms": ms_bp,
+                                    "workload": "Velten confocal, 128^3 voxels x 16384 scan "
+                                                "points x 1024 bins"},
+        "volume render voxel·scanpt/s": {"value": pairs / (ms_vf / 1e3), "ms": ms_vf,
+                                         "workload": "confocal forward, 128^3 (2% occupied) x "
+                                                     "16384 points x 1024 bins"},
+        "volume adjoint voxel·scanpt/s": {"value": pairs / (ms_va / 1e3), "ms": ms_va},
+        "rbf2volume voxel·gaussian/s": {"value": nvox * 4096 / (ms_rf / 1e3), "ms": ms_rf,
+                                        "workload": "4096 Gaussians, 128^3, 1 attribute"},
+        "rbf2volume grad voxel·gaussian/s": {"value": nvox * 4096 / (ms_rg / 1e3),
+                                             "ms": ms_rg},
+    }
+
+
+def batched_metrics(device, count=32, steps=2):
+    """Batched exhaustive mesh forward + backward: 32 meshes with triangle
+    counts log-uniform in [1k, 50k] (lat/long spheres and random boxes),
+    64x64 detector x 16x16 laser points, 2048 bins of 0.005 m; loss
+    0.5 ||transient||^2 per mesh. One graph replay per step (waves within an
+    80 GB transient budget, tiles from the autotuner) against the same work as
+    32 sequential plain calls (forward, then gradient with transient_grad =
+    transient). Unit: (face, detector point, laser point) triples per second."""
+    from totri_gb300 import scenes
+    from totri_gb300.batch import BatchedMeshRenderer
+    from totri_gb300.totri_cpp import render as R
+    s = scenes.batched_exhaustive(count=count)
+    meshes = [tuple(t.to(device) for t in m) for m in s["meshes"]]
+    sp, lp, bd = s["scan_points"].to(device), s["laser_points"].to(device), s["bin_def"]
+    S, L = sp.shape[0], lp.shape[0]
+    triples = sum(m[1].shape[0] for m in meshes) * S * L
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, n):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    t0 = time.time()
+    br = BatchedMeshRenderer(meshes, sp, bd, laser_points=lp, grad="energy", hbm_budget=80e9)
+    setup_s = time.time() - t0
+    br.step()
+    ms_batched = timed(br.step, steps)
+    waves = [len(w.members) for w in br.waves]
+    tiles = {str(k): v for k, v in br.tiles.items()}
+    del br
+    torch.cuda.empty_cache()
+    so = torch.empty((1, 0, 3), device=device)
+
+    def plain():
+        for v, f, m in meshes:
+            v, f, m = v[None], f[None], m[None]
+            out = torch.empty((1, bd.num, S, L), device=device)
+            R.mesh_exhaustive_forward(v, f, m, sp[None], lp[None], so, so, out, bd.width,
+                                      bd.offset, 0)
+            vg, mg = torch.empty_like(v), torch.empty_like(m)
+            R.mesh_exhaustive_grad_verts(v, f, m, sp[None], lp[None], so, so, out, vg, mg,
+                                         bd.width, bd.offset, 0)
+
+    plain()
+    ms_plain = timed(plain, 1)
+    torch.cuda.empty_cache()
+    return {
+        "value": triples / (ms_batched / 1e3), "unit": "triples/s", "ms": ms_batched,
+        "plain_calls": {"value": triples / (ms_plain / 1e3), "ms": ms_plain},
+        "speedup_vs_plain": ms_plain / ms_batched,
+        "workload": "32 meshes, %d triangles in total (log-uniform 1k-50k), 64x64 detector x "
+                    "16x16 laser points, 2048 bins x 0.005 m, fwd+bwd, energy loss" %
+                    sum(m[1].shape[0] for m in meshes),
+        "waves": waves, "tiles": tiles, "setup_s": setup_s,
+    }
+
+
+def serve_metrics(device, num_requests=100, seed=0, slots=4):
+    """Serving mix (60% mesh renders/gradients, 40% Velten backprojections;
+    grids 32^2-256^2, 512-4096 bins, meshes 320-50k faces, volumes 64^3-192^3)
+    through ``totri_gb300.serve.Server`` under an 80 GB budget, against the
+    same requests as back-to-back plain per-call API calls. Each arm returns
+    results to pinned host memory. The server first answers one untimed pass of
+    the request list (its steady state: resident BVHs, cached masks); then
+    (a) all requests submitted at once give the throughput, (b) Poisson
+    arrivals at 70% of that throughput give p50/p99 latency."""
+    from totri_gb300 import scenes
+    from totri_gb300.serve import Request, Server
+    from totri_gb300.totri_cpp import reconstruct as K
+    from totri_gb300.totri_cpp import render as R
+    mix = scenes.serving_mix(num_requests, seed=seed)
+    bins = scenes.SERVE_BINS
+    dev_meshes = {k: tuple(t.to(device) for t in m) for k, m in mix["meshes"].items()}
+    dev_grids = {k: g.to(device) for k, g in mix["grids"].items()}
+    empty = torch.empty((1, 0, 3), device=device)
+    tv, tf, tc = (t.to(device)[None] for t in mix["target"])
+    meas = {}
+    for g, sp in dev_grids.items():
+        for b, bd in enumerate(bins):
+            out = torch.empty((1, bd.num, sp.shape[0]), device=device)
+            R.mesh_confocal_forward(tv, tf, tc, sp[None], empty, out, bd.width, bd.offset, 0)
+            meas["%s_b%d" % (g, b)] = out[0]
+    reqs = mix["requests"]
+
+    def plain(r):
+        sp = dev_grids[r["grid"]][None]
+        bd = bins[r["bins"]]
+        if r["kind"] == "backproject":
+            vd = r["volume"]
+            vol = torch.empty((1,) + tuple(vd.resolution), device=device)
+            K.backprojection_confocal_velten_forward(meas[r["target"]][None], sp, empty, vol,
+                                                     vd.start, vd.end, bd.width, bd.offset)
+            return vol[0].cpu()
+        v, f, c = (t[None] for t in dev_meshes[r["mesh"]])
+        tr = torch.empty((1, bd.num, sp.shape[1]), device=device)
+        R.mesh_confocal_forward(v, f, c, sp, empty, tr, bd.width, bd.offset, 0)
+        if r["kind"] == "render":
+            return tr[0].cpu()
+        diff = tr - meas[r["target"]]
+        loss = (diff * diff).mean()
+        vg, cg = torch.empty_like(v), torch.empty_like(c)
+        R.mesh_confocal_grad_verts(v, f, c, sp, empty, diff.mul_(2.0 / diff.numel()), vg, cg,
+                                   bd.width, bd.offset, 0)
+        return loss.cpu(), vg[0].cpu(), cg[0].cpu()
+
+    plain(reqs[0])
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for r in reqs:
+        plain(r)
+    plain_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()
+
+    def req(r):
+        return Request(r["kind"], r["grid"], mesh=r.get("mesh"), bins=bins[r["bins"]],
+                       target=r.get("target"), volume=r.get("volume"))
+
+    srv = Server(device, hbm_budget=80e9, slots=slots)
+    for k, (v, f, c) in dev_meshes.items():
+        srv.register_mesh(k, v, f, c)
+    for k, sp in dev_grids.items():
+        srv.register_grid(k, sp)
+    for k, t in meas.items():
+        srv.register_measurement(k, t, k.split("_")[0], bins[int(k.split("_b")[1])])
+    resident = srv.budget.resident
+    with srv:
+        for fut in [srv.submit(req(r)) for r in reqs]:  # steady state: BVHs, masks
+            fut.result()
+        srv.completed.clear()
+        t0 = time.perf_counter()
+        for fut in [srv.submit(req(r)) for r in reqs]:
+            fut.result()
+        burst_s = time.perf_counter() - t0
+        srv.completed.clear()
+        rate = 0.7 * len(reqs) / burst_s
+        gaps = np.random.default_rng(seed + 1).exponential(1.0 / rate, len(reqs))
+        futs = []
+        t0 = time.perf_counter()
+        due = t0
+        for r, gap in zip(reqs, gaps):
+            due += gap
+            while time.perf_counter() < due:
+                time.sleep(min(1e-3, max(0.0, due - time.perf_counter())))
+            futs.append(srv.submit(req(r)))
+        for fut in futs:
+            fut.result()
+        poisson_s = time.perf_counter() - t0
+        p50, p99 = srv.latency_ms()
+    kinds = {k: sum(1 for r in reqs if r["kind"] == k) for k in ("render", "grad", "backproject")}
+    out = {
+        "value": len(reqs) / burst_s, "unit": "requests/s",
+        "plain_calls": {"value": len(reqs) / plain_s, "s": plain_s},
+        "speedup_vs_plain": plain_s / burst_s,
+        "poisson": {"rate_per_s": rate, "p50_ms": p50, "p99_ms": p99,
+                    "throughput": len(reqs) / poisson_s},
+        "requests": len(reqs), "kinds": kinds, "slots": slots,
+        "hbm_budget_gb": 80, "resident_gb": resident / 1e9,
+        "peak_admitted_gb": srv.budget.peak / 1e9,
+        "workload": "serving mix: 8 meshes (%s faces), grids 32^2-256^2, 512-4096 bins, "
+                    "volumes 64^3-192^3; steady state (one untimed pass first)" %
+                    ",".join(str(m[1].shape[0]) for m in mix["meshes"].values()),
+    }
+    del srv
+    torch.cuda.empty_cache()
+    return out
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
@@ -234,10 +478,10 @@ def run_reference(args, world, rank):
     from totri_gb300 import scenes
     s = scenes.confocal_differentiable()
     S = s["scan_points"].shape[1]
-    n_sub = 64
-    subset = np.linspace(0, S - 1, n_sub).round().astype(np.int64)
+    n_sub = S  # each step is the whole workload (~4 s on 16 cores)
+    subset = np.arange(S, dtype=np.int64)
     for _ in range(args.warmup):
-        cpu_baseline(s, subset[:8])
+        cpu_baseline(s, subset[::64])
     rates, times = [], []
     for _ in range(args.steps):
         r, dt, pairs = cpu_baseline(s, subset)
@@ -365,14 +609,26 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, device)
     e2e_value = world * pairs * e2e_steps / e2e_s
 
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        secondary = secondary_metrics(device, flush)
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_metrics(device)
+    served = None
+    if rank == 0 and not args.no_serve:
+        served = serve_metrics(device)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        subset = np.linspace(0, S - 1, 64).round().astype(np.int64)
-        cpu_baseline(h, subset[:4])
-        rate, dt, n = cpu_baseline(h, subset)
+        everything = np.arange(S, dtype=np.int64)
+        cpu_baseline(h, everything[::64])
+        runs = [cpu_baseline(h, everything) for _ in range(3)]
+        rate = float(np.median([r[0] for r in runs]))
         cpu = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
-               "sample": "64 of 4096 scan points x 20480 faces (%d pairs, %.1f s): BVH "
-                         "visibility + forward + gradient, FP32, OpenMP" % (n, dt)}
+               "sample": "the whole step (4096 scan points x 20480 faces, %d pairs) 3 times, "
+                         "%.1f s total, median rate: CPU-BVH visibility + forward + gradient, "
+                         "FP32, OpenMP" % (runs[0][2], sum(r[1] for r in runs))}
 
     if rank == 0:
         line = {
@@ -388,6 +644,9 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "clocks": clk, "gpu_launches": launches, "kernels": kernels,
+            "secondary": secondary,
+            "batched": batched,
+            "serve": served,
         }
         print(json.dumps(line), flush=True)
     barrier(world)

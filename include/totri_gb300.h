@@ -73,6 +73,13 @@ void totri_profile_reset(void);
 int totri_profile_read(int max_entries, char* names, int64_t* launches, int64_t* timed,
                        double* total_ms, int* n_entries);
 
+/* Tile-shape overrides chosen by the autotuner (no reference counterpart).
+ * Keys: "mesh.confocal.splat.ts" (scan points per confocal splat CTA: 1, 2,
+ * 4, 8, 16), "mesh.exhaustive.splat.lt" (laser points per exhaustive splat
+ * CTA: 1, 4, 8, 16, 32). 0 restores the built-in heuristic. */
+int totri_tune_set(const char* key, int value);
+int totri_tune_get(const char* key);
+
 /* ----------------------------------------------------------------------- */
 /* render: meshes                                                           */
 
@@ -197,6 +204,46 @@ int totri_mesh_visibility(const totri_array_t* verts, const totri_array_t* faces
  * 2: a BVH walk hit its iteration cap). */
 int totri_mesh_workspace_status(const void* workspace, size_t workspace_bytes,
                                 uint32_t* flags, void* stream);
+
+/* Resident (prepared) meshes. No counterpart in the reference, which builds
+ * its acceleration structure inside every call; these keep one BVH per mesh
+ * batch on the device and visibility masks per wall grid, so that repeated
+ * renders and gradients of the same mesh skip the build and, on a known grid,
+ * the visibility walk. The prepared workspace is totri_mesh_workspace(B, V, F,
+ * 0) bytes and holds the face records, albedo included: a prepared mesh whose
+ * vertices or material change must be prepared again. Mask buffers are
+ * totri_mesh_mask_bytes(B, F, P) bytes, 256-byte aligned, opaque. */
+size_t totri_mesh_mask_bytes(int64_t batch, int64_t num_faces, int64_t num_points);
+
+/* Builds the BVH and face records of verts/faces/material into workspace. */
+int totri_mesh_prepare(const totri_array_t* verts, const totri_array_t* faces,
+                       const totri_array_t* material, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* Visibility masks of a prepared mesh batch for points [B,P,3]. */
+int totri_mesh_prepared_visibility(const totri_array_t* verts, const totri_array_t* faces,
+                                   const totri_array_t* material, const totri_array_t* points,
+                                   const void* workspace, size_t workspace_bytes, void* masks,
+                                   size_t masks_bytes, void* stream);
+
+/* totri_mesh_confocal_forward of a prepared mesh batch with masks computed
+ * for the same scan points (arguments as there; no build, no walk). */
+int totri_mesh_prepared_confocal_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                         const totri_array_t* material,
+                                         const totri_array_t* scan_points,
+                                         const totri_array_t* scan_origin,
+                                         const totri_array_t* transient, float bin_width,
+                                         float bin_offset, const void* workspace,
+                                         size_t workspace_bytes, const void* masks,
+                                         size_t masks_bytes, void* stream);
+
+/* totri_mesh_confocal_grad_verts of a prepared mesh batch with masks. */
+int totri_mesh_prepared_confocal_grad_verts(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* scan_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bin_width, float bin_offset, const void* workspace,
+    size_t workspace_bytes, const void* masks, size_t masks_bytes, void* stream);
 
 /* ----------------------------------------------------------------------- */
 /* render: volumes                                                          */

@@ -52,6 +52,8 @@ _int = ctypes.c_int
 _SIGNATURES = {
     "totri_version": [],
     "totri_last_error": [],
+    "totri_tune_set": [ctypes.c_char_p, _int],
+    "totri_tune_get": [ctypes.c_char_p],
     "totri_profile_enable": [_int],
     "totri_profile_reset": [],
     "totri_profile_read": [_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64),
@@ -66,6 +68,12 @@ _SIGNATURES = {
     "totri_mesh_exhaustive_grad_verts_reuse": [_ArrP] * 10 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_visibility": [_ArrP] * 4 + [_int, _vp, _sz, _vp],
     "totri_mesh_workspace_status": [_vp, _sz, ctypes.POINTER(ctypes.c_uint32), _vp],
+    "totri_mesh_mask_bytes": [_i64, _i64, _i64],
+    "totri_mesh_prepare": [_ArrP] * 3 + [_vp, _sz, _vp],
+    "totri_mesh_prepared_visibility": [_ArrP] * 4 + [_vp, _sz, _vp, _sz, _vp],
+    "totri_mesh_prepared_confocal_forward": [_ArrP] * 6 + [_flt, _flt, _vp, _sz, _vp, _sz, _vp],
+    "totri_mesh_prepared_confocal_grad_verts": [_ArrP] * 8 + [_flt, _flt, _vp, _sz, _vp, _sz,
+                                                              _vp],
     "totri_volume_workspace": [_i64],
     "totri_volume_confocal_forward": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp, _sz, _vp],
     "totri_volume_confocal_grad_volume": [_ArrP] * 3 + [_F3, _F3, _flt, _flt, _vp],
@@ -86,6 +94,7 @@ _RESTYPES = {
     "totri_version": ctypes.c_char_p,
     "totri_last_error": ctypes.c_char_p,
     "totri_mesh_workspace": ctypes.c_size_t,
+    "totri_mesh_mask_bytes": ctypes.c_size_t,
     "totri_volume_workspace": ctypes.c_size_t,
     "totri_profile_reset": None,
 }

@@ -136,12 +136,24 @@ int check_grads(const totri_array_t* vg, const totri_array_t* mg, const MeshArgs
   return TOTRI_OK;
 }
 
+// Mask buffer of a prepared scene: [B][P][ceil(F/32)] words, 256-byte aligned.
+int check_masks(const void* masks, size_t bytes, int64_t B, int64_t F, int64_t P) {
+  const size_t need = mesh::mask_bytes(B, F, P);
+  if (!masks || bytes < need)
+    return fail(TOTRI_ERR_WORKSPACE, "mask buffer of " + std::to_string(need) +
+                                         " bytes required, got " + std::to_string(bytes));
+  if ((reinterpret_cast<uintptr_t>(masks) & 255) != 0)
+    return fail(TOTRI_ERR_WORKSPACE, "mask buffer must be 256-byte aligned");
+  return TOTRI_OK;
+}
+
 int confocal_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
                        const totri_array_t* material, const totri_array_t* scan_points,
                        const totri_array_t* scan_origin, const totri_array_t* transient_grad,
                        const totri_array_t* verts_grad, const totri_array_t* material_grad,
                        float bin_width, float bin_offset, void* ws, size_t ws_bytes,
-                       void* stream_, bool reuse) {
+                       void* stream_, bool reuse, void* masks = nullptr,
+                       size_t masks_bytes = 0) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   MeshArgs a;
   TOTRI_TRY(check_mesh(verts, faces, material, a));
@@ -159,10 +171,16 @@ int confocal_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
   TOTRI_TRY(zero3(verts_grad, stream));
   TOTRI_TRY(zero3(material_grad, stream));
   if (a.F == 0 || S == 0 || T == 0 || a.B == 0 || (!out.vg && !out.mg)) return TOTRI_OK;
-  const mesh::Layout L = mesh::layout(a.B, a.F, S);
-  TOTRI_TRY(check_workspace(ws, ws_bytes, L.total));
-  const mesh::Scene sc = mesh::scene_from_workspace(ws, a.B, a.F, S);
-  if (!reuse) {
+  mesh::Scene sc;
+  if (masks) {  // prepared scene, masks from totri_mesh_prepared_visibility
+    TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(a.B, a.F, 0).total));
+    TOTRI_TRY(check_masks(masks, masks_bytes, a.B, a.F, S));
+    sc = mesh::scene_with_masks(ws, a.B, a.F, masks, S);
+  } else {
+    TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(a.B, a.F, S).total));
+    sc = mesh::scene_from_workspace(ws, a.B, a.F, S);
+  }
+  if (!reuse && !masks) {
     TOTRI_TRY(mesh::build_scene(sc, a.in, stream));
     TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)S, 0, false, stream));
   }
@@ -410,6 +428,86 @@ int totri_mesh_visibility(const totri_array_t* verts, const totri_array_t* faces
   TOTRI_TRY(mesh::build_scene(sc, a.in, stream));
   TOTRI_TRY(mesh::launch_visibility(sc, view3f(points), (int)P, 0, brute_force != 0, stream));
   return mesh::launch_mask_unsort(sc, (int)P, static_cast<uint32_t*>(mask->data), stream);
+}
+
+size_t totri_mesh_mask_bytes(int64_t batch, int64_t num_faces, int64_t num_points) {
+  if (batch <= 0 || num_faces <= 0 || num_points < 0) return 0;
+  return mesh::mask_bytes(batch, num_faces, num_points);
+}
+
+int totri_mesh_prepare(const totri_array_t* verts, const totri_array_t* faces,
+                       const totri_array_t* material, void* ws, size_t ws_bytes, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  MeshArgs a;
+  TOTRI_TRY(check_mesh(verts, faces, material, a));
+  if (a.F == 0 || a.B == 0) return TOTRI_OK;
+  TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(a.B, a.F, 0).total));
+  return mesh::build_scene(mesh::scene_from_workspace(ws, a.B, a.F, 0), a.in, stream);
+}
+
+int totri_mesh_prepared_visibility(const totri_array_t* verts, const totri_array_t* faces,
+                                   const totri_array_t* material, const totri_array_t* points,
+                                   const void* ws, size_t ws_bytes, void* masks,
+                                   size_t masks_bytes, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  MeshArgs a;
+  TOTRI_TRY(check_mesh(verts, faces, material, a));
+  int64_t P;
+  TOTRI_TRY(check_points(points, "points", a.B, P));
+  if (a.F == 0 || P == 0 || a.B == 0) return TOTRI_OK;
+  if (P >= (int64_t)1 << 30) return fail(TOTRI_ERR_UNSUPPORTED, "too many points");
+  TOTRI_TRY(check_workspace(const_cast<void*>(ws), ws_bytes, mesh::layout(a.B, a.F, 0).total));
+  TOTRI_TRY(check_masks(masks, masks_bytes, a.B, a.F, P));
+  const mesh::Scene sc = mesh::scene_with_masks(const_cast<void*>(ws), a.B, a.F, masks, P);
+  return mesh::launch_visibility(sc, view3f(points), (int)P, 0, false, stream);
+}
+
+int totri_mesh_prepared_confocal_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                         const totri_array_t* material,
+                                         const totri_array_t* scan_points,
+                                         const totri_array_t* scan_origin,
+                                         const totri_array_t* transient, float bin_width,
+                                         float bin_offset, const void* ws, size_t ws_bytes,
+                                         const void* masks, size_t masks_bytes, void* stream_) {
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  MeshArgs a;
+  TOTRI_TRY(check_mesh(verts, faces, material, a));
+  int64_t S;
+  int has_origin;
+  TOTRI_TRY(check_points(scan_points, "scan_points", a.B, S));
+  TOTRI_TRY(check_origin(scan_origin, "scan_origin", a.B, S, has_origin));
+  TOTRI_TRY(check_array(transient, "transient", 3, TOTRI_FLOAT32));
+  TOTRI_TRY(check_dim(transient, "transient", 0, a.B));
+  TOTRI_TRY(check_dim(transient, "transient", 2, S));
+  TOTRI_TRY(check_contiguous(transient, "transient"));
+  const int64_t T = transient->shape[1];
+  if (numel(transient) == 0) return TOTRI_OK;
+  if (a.F == 0) {
+    TOTRI_CUDA(cudaMemsetAsync(transient->data, 0, sizeof(float) * numel(transient), stream));
+    return TOTRI_OK;
+  }
+  if (S >= (int64_t)1 << 30 || T >= (int64_t)1 << 30)
+    return fail(TOTRI_ERR_UNSUPPORTED, "too many scan points or bins");
+  TOTRI_TRY(check_workspace(const_cast<void*>(ws), ws_bytes, mesh::layout(a.B, a.F, 0).total));
+  TOTRI_TRY(check_masks(masks, masks_bytes, a.B, a.F, S));
+  const mesh::Scene sc =
+      mesh::scene_with_masks(const_cast<void*>(ws), a.B, a.F, const_cast<void*>(masks), S);
+  return mesh::launch_confocal_splat(sc, view3f(scan_points), view3f(scan_origin), has_origin,
+                                     static_cast<float*>(transient->data), (int)T, (int)S,
+                                     bin_width, bin_offset, stream);
+}
+
+int totri_mesh_prepared_confocal_grad_verts(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* scan_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bin_width, float bin_offset, const void* ws,
+    size_t ws_bytes, const void* masks, size_t masks_bytes, void* stream) {
+  if (!masks) return fail(TOTRI_ERR_WORKSPACE, "mask buffer missing");
+  return confocal_grad_impl(verts, faces, material, scan_points, scan_origin, transient_grad,
+                            verts_grad, material_grad, bin_width, bin_offset,
+                            const_cast<void*>(ws), ws_bytes, stream, true,
+                            const_cast<void*>(masks), masks_bytes);
 }
 
 int totri_mesh_workspace_status(const void* ws, size_t ws_bytes, uint32_t* flags, void* stream_) {

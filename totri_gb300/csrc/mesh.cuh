@@ -118,6 +118,21 @@ inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
   return s;
 }
 
+// A scene whose BVH and face records live in `ws` (laid out for zero wall
+// points) and whose visibility masks [B][P][nch] live in a separate buffer:
+// the resident form, where one BVH serves many wall grids.
+inline Scene scene_with_masks(void* ws, int64_t B, int64_t F, void* masks, int64_t P) {
+  Scene s = scene_from_workspace(ws, B, F, 0);
+  s.P = (int)P;
+  s.mask = static_cast<uint32_t*>(masks);
+  return s;
+}
+
+inline size_t mask_bytes(int64_t B, int64_t F, int64_t P) {
+  const int64_t Fc = F > 0 ? F : 1;
+  return sizeof(uint32_t) * (size_t)B * (size_t)P * (size_t)((Fc + 31) / 32);
+}
+
 // ---------------------------------------------------------------------------
 // Device helpers.
 
@@ -282,45 +297,39 @@ __device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, 
   return true;
 }
 
-// One ray of the persistent visibility walk, advanced one BVH node per step.
-struct RayState {
-  fv3 o, dir, inv, oinv;
-  float tf, tmax;
-  int k, f;
-  int node, sp;
-  int it;
-};
-
-// Sets up the ray from o to the centroid of face k. Returns 0 when the ray is
-// decided without a walk (not visible), 1 when the face is visible with no
-// walk needed (a single face), 2 when the walk must run.
-__device__ __forceinline__ int ray_setup(const Scene& sc, int b, int n, int k, fv3 o,
-                                         RayState& r) {
-  const Target tg = load_target(sc, b, k);
-  const fv3 D = xsub3(tg.c, o);
-  const float dist = xlen(D);
-  if (!(dist >= 1e-6f)) return 0;
-  r.o = o;
-  r.dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
-  r.tmax = xadd(xmul(dist, 1.01f), 1e-3f);
-  r.k = k;
-  r.f = tg.f;
-  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, r.dir, r.tmax, r.tf)) return 0;
-  if (n == 1) return 1;
-  r.inv = mkv(safe_inv(r.dir.x), safe_inv(r.dir.y), safe_inv(r.dir.z));
-  r.oinv = mkv(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
-  r.node = 0;
-  r.sp = 0;
-  r.it = 0;
-  return 2;
-}
-
-// One node of the walk. Returns 0 (occluded), 1 (stack empty: visible) or
-// 2 (continue). Same decisions as target_visible.
-__device__ __forceinline__ int ray_step(const Scene& sc, int b, int n, RayState& r, int* stack,
-                                        uint32_t* status) {
+// Warp-cooperative visibility of 32 targets seen from one wall point: lane i
+// holds the ray from o to the centroid of its target (valid lanes only). The
+// warp walks the BVH as one packet: it enters a node when the slab test of any
+// still-undecided lane passes, and each lane tests a leaf triangle only when
+// its own slab test of that leaf passes. Every node a lane's own walk would
+// enter is entered, so each lane meets every occluder its own walk meets and
+// the answer per lane is the one target_visible gives (no occluder can be
+// invented: occlusion is decided by the exact triangle test alone). Node and
+// leaf records are read at one address per warp; the stack is warp-uniform and
+// held in registers, entry i in lane i % 32. All 32 lanes must call this.
+__device__ __forceinline__ bool packet_visible(const Scene& sc, int b, int n, bool valid,
+                                               const Target& tg, fv3 o, uint32_t* status) {
+  constexpr uint32_t kAll = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  bool active = false;
+  fv3 dir = mkv(1.f, 0.f, 0.f);
+  float tmax = 0.f, tf = 0.f;
+  if (valid) {
+    const fv3 D = xsub3(tg.c, o);
+    const float dist = xlen(D);
+    if (dist >= 1e-6f) {
+      dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+      tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+      active = tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf);
+    }
+  }
+  if (n == 1) return active;
+  bool vis = active;
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const int k = tg.k, f = tg.f;
   auto occludes = [&](int kk) -> bool {
-    if (kk == r.k) return false;
+    if (kk == k) return false;
     if (kk < 0 || kk >= n) {
       atomicOr(status, kStatusTraversalCap);
       return false;
@@ -328,41 +337,59 @@ __device__ __forceinline__ int ray_step(const Scene& sc, int b, int n, RayState&
     const float4* q = tri_at(sc, b, kk);
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
     float tq;
-    if (!tri_hit(q0, q1, q2, q3, r.o, r.dir, r.tmax, tq)) return false;
-    return tq < r.tf || (tq == r.tf && __float_as_int(q3.w) < r.f);
+    if (!tri_hit(q0, q1, q2, q3, o, dir, tmax, tq)) return false;
+    return tq < tf || (tq == tf && __float_as_int(q3.w) < f);
   };
-  if (r.node < 0 || r.node >= n - 1 || ++r.it > 2 * n + 64) {
-    atomicOr(status, kStatusTraversalCap);
-    return 1;
+  int s_lo = 0, s_hi = 0;  // stack entries [0, 32) and [32, 64), one per lane
+  int sp = 0, node = 0;
+  const int cap = 2 * n + 64;
+  for (int it = 0;; ++it) {
+    if (__ballot_sync(kAll, active) == 0) break;
+    if (it >= cap || node < 0 || node >= n - 1) {  // malformed tree (warp-uniform)
+      if (lane == 0) atomicOr(status, kStatusTraversalCap);
+      break;
+    }
+    const float4* nd = node_at(sc, b, node);
+    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+    float tn0 = 0.f, tn1 = 0.f;
+    bool h0 = active && slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
+    bool h1 = active && slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    if (c0 < 0) {
+      if (h0 && occludes(~c0)) active = vis = false;
+      h0 = false;
+    }
+    if (c1 < 0) {
+      if (h1 && occludes(~c1)) active = vis = false;
+      h1 = false;
+    }
+    const uint32_t m0 = __ballot_sync(kAll, h0), m1 = __ballot_sync(kAll, h1);
+    if (m0 && m1) {
+      // nearer child first, by lane vote
+      const uint32_t pref0 = __ballot_sync(kAll, h0 && (!h1 || tn0 <= tn1));
+      const bool first0 = 2 * __popc(pref0) >= __popc(m0 | m1);
+      const int later = first0 ? c1 : c0;
+      if (sp < 64) {
+        if (lane == (sp & 31)) {
+          if (sp < 32) s_lo = later;
+          else s_hi = later;
+        }
+        ++sp;
+      } else if (lane == 0) {
+        atomicOr(status, kStatusTraversalCap);
+      }
+      node = first0 ? c0 : c1;
+    } else if (m0) {
+      node = c0;
+    } else if (m1) {
+      node = c1;
+    } else {
+      if (sp == 0) break;
+      --sp;
+      node = __shfl_sync(kAll, sp < 32 ? s_lo : s_hi, sp & 31);
+    }
   }
-  const float4* nd = node_at(sc, b, r.node);
-  const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-  float tn0, tn1;
-  bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, r.inv, r.oinv, r.tf, tn0);
-  bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, r.inv, r.oinv, r.tf, tn1);
-  const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-  if (h0 && c0 < 0) {
-    if (occludes(~c0)) return 0;
-    h0 = false;
-  }
-  if (h1 && c1 < 0) {
-    if (occludes(~c1)) return 0;
-    h1 = false;
-  }
-  if (h0 && h1) {
-    const bool first0 = tn0 <= tn1;
-    if (r.sp < 64) stack[r.sp++] = first0 ? c1 : c0;
-    else atomicOr(status, kStatusTraversalCap);
-    r.node = first0 ? c0 : c1;
-  } else if (h0) {
-    r.node = c0;
-  } else if (h1) {
-    r.node = c1;
-  } else {
-    if (r.sp == 0) return 1;
-    r.node = stack[--r.sp];
-  }
-  return 2;
+  return vis;
 }
 
 }  // namespace mesh

@@ -11,12 +11,14 @@
 //    splatting into a shared-memory histogram [T][TS] with shared atomics, and
 //    flushes the tile with coalesced float4 stores (no global atomics, no
 //    separate zero fill);
-//  * the gradient gives each CTA one 32-face mask word and walks all scan
-//    points (lanes over s, so transient_grad reads are row-coalesced), keeps
+//  * the gradient gives each CTA one 32-face mask word and a slice of the scan
+//    points (lanes over s, so transient_grad reads are row-coalesced; slices
+//    keep every SM busy when there are few faces), keeps
 //    the per-face gradient in registers, reduces it across the warp and issues
 //    12 atomics per face instead of 9 + 3M per visible pair.
 #include "mesh.cuh"
 #include "mesh_kernels.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace mesh {
@@ -25,24 +27,40 @@ namespace {
 
 // One warp per (wall point, 32 Morton-consecutive faces): the 32 rays share
 // their origin and end on a compact patch of the surface, so they walk
-// largely the same BVH nodes.
-template <bool kBrute>
+// largely the same BVH nodes. kVisRay lets each lane walk alone
+// (target_visible; the default), kVisPacket walks them as one warp packet
+// (packet_visible; about twice the node visits on the 20,480-face sphere
+// seen from a 64x64 wall, so only the tuner picks it), kVisBrute tests every
+// face; all three give the same bits.
+constexpr int kVisBrute = 0;
+constexpr int kVisRay = 1;
+constexpr int kVisPacket = 2;
+
+template <int kMode>
 __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t per_b = (int64_t)P * sc.nch;
-  if (gw >= per_b * sc.B) return;
+  if (gw >= per_b * sc.B) return;  // whole warp
   const int b = (int)(gw / per_b);
   const int64_t rem = gw - (int64_t)b * per_b;
   const int p = (int)(rem / sc.nch);
   const int ch = (int)(rem - (int64_t)p * sc.nch);
   const int n = sc.meta[b].n;
   const int k = ch * 32 + lane;
+  const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
   bool vis = false;
-  if (k < n) {
-    const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
+  if (kMode == kVisPacket) {
+    if (ch * 32 < n) {  // warp-uniform
+      Target tg{};
+      tg.k = k;
+      if (k < n) tg = load_target(sc, b, k);
+      vis = packet_visible(sc, b, n, k < n, tg, o, sc.status);
+    }
+  } else if (k < n) {
     int cache = -1;
-    vis = target_visible<kBrute>(sc, b, n, load_target(sc, b, k), o, cache, sc.status);
+    vis = target_visible<kMode == kVisBrute>(sc, b, n, load_target(sc, b, k), o, cache,
+                                             sc.status);
   }
   const uint32_t word = __ballot_sync(0xffffffffu, vis);
   if (lane == 0) sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
@@ -182,7 +200,10 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
   const int ch = blockIdx.x;
   const int n = sc.meta[b].n;
   if (ch * 32 >= n) return;
-  for (int s = threadIdx.x; s < S; s += blockDim.x)
+  // scan-point slice [s0, s1) of this CTA (gridDim.z slices)
+  const int s0 = (int)((int64_t)S * blockIdx.z / gridDim.z);
+  const int s1 = (int)((int64_t)S * (blockIdx.z + 1) / gridDim.z);
+  for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x)
     mcol[s] = sc.mask[((size_t)b * sc.P + s) * sc.nch + ch];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -196,7 +217,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
     const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
     fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
     float accm = 0.f;
-    for (int s = lane; s < S; s += 32) {
+    for (int s = s0 + lane; s < s1; s += 32) {
       if (!((mcol[s] >> j) & 1u)) continue;
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       float od = 0.f;
@@ -211,83 +232,6 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
       accm += dm;
     }
     scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
-  }
-}
-
-// Persistent BVH walk: each warp owns kVisUnits mask words (32 rays each, in
-// (batch, point, face chunk) order, so consecutive rays share an origin and
-// end on neighbouring faces). A lane whose ray finishes takes the next ray of
-// the warp's pool; the warp keeps stepping while at least kVisRefill lanes are
-// busy, then refills idle lanes together (rays decided at set-up free their
-// lane at once). Visible rays set their bit in a shared word per unit.
-constexpr int kVisUnits = 16;
-constexpr int kVisWarps = 8;
-constexpr int kVisRefill = 20;
-
-__global__ void __launch_bounds__(256) visibility_walk_kernel(Scene sc, View3f pts, int P,
-                                                              int row0) {
-  __shared__ uint32_t words[kVisWarps][kVisUnits];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t per_b = (int64_t)P * sc.nch;
-  const int64_t total_units = per_b * sc.B;
-  const int64_t u0 = ((int64_t)blockIdx.x * kVisWarps + warp) * kVisUnits;
-  if (u0 >= total_units) return;  // whole warp
-  if (lane < kVisUnits) words[warp][lane] = 0;
-  __syncwarp();
-  const int nrays = (int)min((int64_t)kVisUnits, total_units - u0) * 32;
-  const uint32_t lt = (1u << lane) - 1u;
-  int next = 0;  // warp-uniform
-  bool busy = false;
-  int ray = 0, b = 0, n = 0;
-  RayState r;
-  int stack[64];
-  while (true) {
-    // refill idle lanes; a ray decided at set-up leaves its lane idle for the next round
-    while (next < nrays) {
-      const bool idle = !busy;
-      const uint32_t im = __ballot_sync(0xffffffffu, idle);
-      if (im == 0) break;
-      const int mine = next + __popc(im & lt);
-      next += __popc(im);
-      if (idle && mine < nrays) {
-        ray = mine;
-        const int64_t G = u0 + (ray >> 5);
-        b = (int)(G / per_b);
-        const int64_t rem = G - (int64_t)b * per_b;
-        const int p = (int)(rem / sc.nch);
-        const int ch = (int)(rem - (int64_t)p * sc.nch);
-        n = sc.meta[b].n;
-        const int k = ch * 32 + (ray & 31);
-        if (k < n) {
-          const fv3 o = mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2));
-          const int st = ray_setup(sc, b, n, k, o, r);
-          if (st == 2) busy = true;
-          else if (st == 1) atomicOr(&words[warp][ray >> 5], 1u << (ray & 31));
-        }
-      }
-    }
-    if (__ballot_sync(0xffffffffu, busy) == 0) break;
-    // walk while enough lanes are busy (or until all are done once the pool is empty)
-    while (true) {
-      if (busy) {
-        const int st = ray_step(sc, b, n, r, stack, sc.status);
-        if (st != 2) {
-          busy = false;
-          if (st == 1) atomicOr(&words[warp][ray >> 5], 1u << (ray & 31));
-        }
-      }
-      const int nb = __popc(__ballot_sync(0xffffffffu, busy));
-      if (nb == 0 || (next < nrays && nb < kVisRefill)) break;
-    }
-  }
-  __syncwarp();
-  if (lane < kVisUnits && u0 + lane < total_units) {
-    const int64_t G = u0 + lane;
-    const int bb = (int)(G / per_b);
-    const int64_t rem = G - (int64_t)bb * per_b;
-    const int p = (int)(rem / sc.nch);
-    const int ch = (int)(rem - (int64_t)p * sc.nch);
-    sc.mask[((size_t)bb * sc.P + row0 + p) * sc.nch + ch] = words[warp][lane];
   }
 }
 
@@ -317,15 +261,16 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
                       cudaStream_t stream) {
   const int64_t units = (int64_t)sc.B * P * sc.nch;
   if (units == 0) return TOTRI_OK;
+  const unsigned blocks = (unsigned)ceil_div(units * 32, 256);
   if (brute) {
-    const int64_t blocks = ceil_div(units * 32, 256);
     TOTRI_KERNEL("mesh visibility brute", stream,
-                 visibility_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(sc, pts, P, row0));
-  } else {
-    const int64_t blocks = ceil_div(units, (int64_t)kVisUnits * kVisWarps);
+                 visibility_kernel<kVisBrute><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
+  } else if (tune::get("mesh.visibility.mode") == kVisPacket) {
     TOTRI_KERNEL("mesh visibility", stream,
-                 visibility_walk_kernel<<<(unsigned)blocks, 32 * kVisWarps, 0, stream>>>(
-                     sc, pts, P, row0));
+                 visibility_kernel<kVisPacket><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
+  } else {
+    TOTRI_KERNEL("mesh visibility", stream,
+                 visibility_kernel<kVisRay><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
   }
   return TOTRI_OK;
 }
@@ -352,6 +297,19 @@ int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, i
                           float* transient, int T, int S, float bw, float bo,
                           cudaStream_t stream) {
   const size_t budget = 200 * 1024;
+  const int want = tune::get("mesh.confocal.splat.ts");
+  if (want > 0) {
+    if ((size_t)T * want * 4 > budget)
+      return fail(TOTRI_ERR_INVALID_ARGUMENT, "tuned scan tile too large for the bin count");
+    switch (want) {
+      case 1: return launch_splat_ts<1>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+      case 2: return launch_splat_ts<2>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+      case 4: return launch_splat_ts<4>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+      case 8: return launch_splat_ts<8>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+      case 16: return launch_splat_ts<16>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
+      default: return fail(TOTRI_ERR_INVALID_ARGUMENT, "scan tile must be 1, 2, 4, 8 or 16");
+    }
+  }
   if ((size_t)T * 8 * 4 <= budget && S >= 8 * 152)
     return launch_splat_ts<8>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
   if ((size_t)T * 4 * 4 <= budget && S >= 4 * 152)
@@ -374,7 +332,8 @@ int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, in
                                     (int)smem));
     configured = (int)smem;
   }
-  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B);
+  const int split = tune::grad_split("mesh.confocal.grad.split", (int64_t)sc.nch * sc.B, S);
+  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh confocal grad", stream,
                grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, tgrad, T, S, bw,
                                                         bo, out));

@@ -9,10 +9,12 @@
 // are computed once (S + L rows of the shared mask buffer) and each triple is
 // their AND. The forward gives each CTA one scan point and a tile of laser
 // points with a [T][tile] shared histogram flushed as rows of the [T][S][L]
-// output; the gradient gives each CTA 32 faces and walks every (s, l) pair.
+// output; the gradient gives each CTA 32 faces and a slice of scan points and
+// walks every (s, l) pair of the slice.
 #include "capi_common.cuh"
 #include "mesh.cuh"
 #include "mesh_kernels.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace mesh {
@@ -177,8 +179,11 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
   const int ch = blockIdx.x;
   const int n = sc.meta[b].n;
   if (ch * 32 >= n) return;
+  // scan-point slice [s0, s1) of this CTA (gridDim.z slices); all laser rows
+  const int s0 = (int)((int64_t)S * blockIdx.z / gridDim.z);
+  const int s1 = (int)((int64_t)S * (blockIdx.z + 1) / gridDim.z);
   for (int i = threadIdx.x; i < S + L; i += blockDim.x)
-    mcol[i] = sc.mask[((size_t)b * sc.P + i) * sc.nch + ch];
+    if (i >= S || (i >= s0 && i < s1)) mcol[i] = sc.mask[((size_t)b * sc.P + i) * sc.nch + ch];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const float* tgb = tgrad + (size_t)b * T * S * L;
@@ -192,7 +197,7 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
     const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
     fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
     float accm = 0.f;
-    for (int s = 0; s < S; ++s) {
+    for (int s = s0; s < s1; ++s) {
       if (!((mcol[s] >> j) & 1u)) continue;
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       for (int l = lane; l < L; l += 32) {
@@ -234,6 +239,19 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
                             const Origins& org, int S, int L, float* out, int T, float bw,
                             float bo, cudaStream_t stream) {
   const size_t budget = 200 * 1024;
+  const int want = tune::get("mesh.exhaustive.splat.lt");
+  if (want > 0) {
+    if ((size_t)T * want * 4 > budget)
+      return fail(TOTRI_ERR_INVALID_ARGUMENT, "tuned laser tile too large for the bin count");
+    switch (want) {
+      case 1: return launch_exh_splat<1>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+      case 4: return launch_exh_splat<4>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+      case 8: return launch_exh_splat<8>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+      case 16: return launch_exh_splat<16>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+      case 32: return launch_exh_splat<32>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+      default: return fail(TOTRI_ERR_INVALID_ARGUMENT, "laser tile must be 1, 4, 8, 16 or 32");
+    }
+  }
   if ((size_t)T * 16 * 4 <= budget && L >= 16)
     return launch_exh_splat<16>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
   if ((size_t)T * 4 * 4 <= budget && L >= 4)
@@ -254,7 +272,9 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                                     (int)smem));
     configured = (int)smem;
   }
-  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B);
+  const int split =
+      tune::grad_split("mesh.exhaustive.grad.split", (int64_t)sc.nch * sc.B, S);
+  const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh exhaustive grad", stream,
                exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T, bw,
                                                             bo, out));

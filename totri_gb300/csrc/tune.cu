@@ -1,0 +1,60 @@
+// Tile-shape overrides set by the autotuner (totri_gb300/autotune.py). A value
+// of 0 (or an unknown key) leaves the launcher's own heuristic in charge.
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "tune.cuh"
+
+namespace totri {
+namespace tune {
+namespace {
+std::mutex g_mu;
+std::map<std::string, int>& table() {
+  static std::map<std::string, int> t;
+  return t;
+}
+}  // namespace
+
+int get(const char* key) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = table().find(key);
+  return it == table().end() ? 0 : it->second;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    return 152;
+  return n;
+}
+
+int grad_split(const char* key, int64_t ctas, int S) {
+  const int most = S >= 64 ? S / 64 : 1;
+  const int want = get(key);
+  if (want > 0) return want < most ? want : most;
+  if (ctas <= 0) return 1;
+  const int64_t target = (int64_t)sm_count() * 8;
+  const int64_t split = (target + ctas - 1) / ctas;
+  return (int)(split < most ? split : most);
+}
+
+}  // namespace tune
+}  // namespace totri
+
+extern "C" {
+
+int totri_tune_set(const char* key, int value) {
+  if (!key) return totri::fail(TOTRI_ERR_INVALID_ARGUMENT, "tuning key is null");
+  std::lock_guard<std::mutex> lk(totri::tune::g_mu);
+  if (value == 0) totri::tune::table().erase(key);
+  else totri::tune::table()[key] = value;
+  return TOTRI_OK;
+}
+
+int totri_tune_get(const char* key) { return key ? totri::tune::get(key) : 0; }
+
+}  // extern "C"

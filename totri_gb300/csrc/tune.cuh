@@ -1,0 +1,18 @@
+// Tile-shape overrides (see tune.cu). Keys:
+//   "mesh.confocal.splat.ts"    scan points per confocal splat CTA (1,2,4,8,16)
+//   "mesh.exhaustive.splat.lt"  laser points per exhaustive splat CTA (1,4,8,16,32)
+//   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
+//   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk
+//   "mesh.confocal.grad.split"  scan-point slices per confocal gradient chunk
+//   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
+#pragma once
+
+namespace totri {
+namespace tune {
+int get(const char* key);  // 0 when unset
+int sm_count();            // multiprocessors of the current device
+// Slices of the scan-point loop for a gradient grid of `ctas` CTAs: enough to
+// give every SM several CTAs, at most one per 64 points (tuned value first).
+int grad_split(const char* key, int64_t ctas, int S);
+}  // namespace tune
+}  // namespace totri

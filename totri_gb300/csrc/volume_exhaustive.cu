@@ -11,6 +11,7 @@
 #include <string>
 
 #include "capi_common.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace vexh {
@@ -240,7 +241,16 @@ int totri_volume_exhaustive_forward(const totri_array_t* vol, const totri_array_
                      vb, nv, list, count));
     float* out = static_cast<float*>(transient->data);
     const size_t budget = 200 * 1024;
-    if ((size_t)g.T * 32 * 4 <= budget && L >= 32)
+    const int want = tune::get("volume.exhaustive.lt");
+    if (want == 1 || want == 8 || want == 32) {
+      if ((size_t)g.T * want * 4 > budget)
+        return fail(TOTRI_ERR_INVALID_ARGUMENT, "tuned laser tile too large for the bin count");
+      if (want == 32) TOTRI_TRY(launch_fwd<32>(g, b, vb, list, count, sp, lp, out, stream));
+      else if (want == 8) TOTRI_TRY(launch_fwd<8>(g, b, vb, list, count, sp, lp, out, stream));
+      else TOTRI_TRY(launch_fwd<1>(g, b, vb, list, count, sp, lp, out, stream));
+    } else if (want != 0) {
+      return fail(TOTRI_ERR_INVALID_ARGUMENT, "laser tile must be 1, 8 or 32");
+    } else if ((size_t)g.T * 32 * 4 <= budget && L >= 32)
       TOTRI_TRY(launch_fwd<32>(g, b, vb, list, count, sp, lp, out, stream));
     else if ((size_t)g.T * 8 * 4 <= budget && L >= 8)
       TOTRI_TRY(launch_fwd<8>(g, b, vb, list, count, sp, lp, out, stream));

@@ -166,3 +166,125 @@ def rbf_set(n, seed, start=(-0.5, -0.5, 0.5), end=(0.5, 0.5, 1.5)):
     s = g.uniform(0.01, 0.05, size=(n, 1))
     w = g.uniform(0.0, 1.0, size=(n, 1))
     return torch.from_numpy(np.concatenate([c, s, w], axis=1).astype(np.float32))[None]
+
+
+def uv_sphere(target_faces, seed, radius=0.3, center=(0.0, 0.0, 1.0), amplitude=0.05):
+    """Latitude/longitude sphere with about `target_faces` triangles (n rings x
+    2n segments: 4n(n-1) faces), radial displacement amplitude * (degree-4 SH
+    noise) and albedo U[0.5, 1]."""
+    n = max(3, int(round(0.5 + math.sqrt(target_faces / 4.0 + 0.25))))
+    seg = 2 * n
+    theta = np.pi * np.arange(1, n) / n
+    phi = 2.0 * np.pi * np.arange(seg) / seg
+    st, ct = np.sin(theta)[:, None], np.cos(theta)[:, None]
+    ring = np.stack([st * np.cos(phi)[None], st * np.sin(phi)[None],
+                     np.broadcast_to(ct, (n - 1, seg))], -1).reshape(-1, 3)
+    dirs = np.concatenate([[[0.0, 0.0, 1.0]], ring, [[0.0, 0.0, -1.0]]])
+    top, bot = 0, dirs.shape[0] - 1
+    idx = lambda r, j: 1 + r * seg + (j % seg)  # noqa: E731
+    faces = []
+    for j in range(seg):
+        faces.append((top, idx(0, j), idx(0, j + 1)))
+        faces.append((bot, idx(n - 2, j + 1), idx(n - 2, j)))
+    for r in range(n - 2):
+        for j in range(seg):
+            a, b, c, d = idx(r, j), idx(r, j + 1), idx(r + 1, j), idx(r + 1, j + 1)
+            faces += [(a, c, b), (b, c, d)]
+    rad = radius + amplitude * radial_noise(dirs, seed)
+    albedo = rng(seed + 7919).uniform(0.5, 1.0, size=dirs.shape[0])
+    return _mesh_tensors(dirs * rad[:, None] + np.array(center), np.array(faces), albedo)
+
+
+def random_box(target_faces, seed, center=(0.0, 0.0, 1.0)):
+    """Randomly sized and rotated box (edges U[0.2, 0.6] m) whose six sides are
+    m x m grids of quads (12 m^2 triangles, m chosen for `target_faces`),
+    albedo U[0.5, 1]."""
+    g = rng(seed)
+    m = max(1, int(round(math.sqrt(target_faces / 12.0))))
+    half = g.uniform(0.1, 0.3, size=3)
+    q, _ = np.linalg.qr(g.standard_normal((3, 3)))
+    u = np.linspace(-1.0, 1.0, m + 1)
+    uu, vv = np.meshgrid(u, u, indexing="ij")
+    verts, faces = [], []
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            p = np.zeros((m + 1, m + 1, 3))
+            p[..., axis] = sign
+            p[..., (axis + 1) % 3] = uu
+            p[..., (axis + 2) % 3] = vv
+            base = sum(v.shape[0] for v in verts)
+            verts.append(p.reshape(-1, 3))
+            for i in range(m):
+                for j in range(m):
+                    a = base + i * (m + 1) + j
+                    b, c, d = a + 1, a + m + 1, a + m + 2
+                    faces += [(a, c, b), (b, c, d)] if sign > 0 else [(a, b, c), (b, d, c)]
+    v = np.concatenate(verts) * half
+    v = v @ q.T + np.array(center)
+    albedo = g.uniform(0.5, 1.0, size=v.shape[0])
+    return _mesh_tensors(v, np.array(faces), albedo)
+
+
+def batched_exhaustive(count=32, seed=0, lo=1000, hi=50000):
+    """Batched exhaustive workload: `count` meshes with triangle counts
+    log-uniform in [lo, hi] (alternately displaced lat/long spheres and random
+    boxes, centres jittered around (0, 0, 1)); 64x64 detector points and
+    16x16 laser points on [-1,1]^2; 2048 bins of 0.005 m."""
+    g = rng(seed)
+    meshes = []
+    for i in range(count):
+        nf = int(round(math.exp(g.uniform(math.log(lo), math.log(hi)))))
+        c = (float(g.uniform(-0.2, 0.2)), float(g.uniform(-0.2, 0.2)), float(g.uniform(0.8, 1.2)))
+        if i % 2 == 0:
+            v, f, a = uv_sphere(nf, seed * 1000 + i, radius=float(g.uniform(0.15, 0.35)), center=c)
+        else:
+            v, f, a = random_box(nf, seed * 1000 + i, center=c)
+        meshes.append((v[0], f[0], a[0]))
+    return dict(meshes=meshes, scan_points=wall_grid(64)[0], laser_points=wall_grid(16)[0],
+                bin_def=BinDef(0.005, 0.0, 2048))
+
+
+SERVE_BINS = (BinDef(0.01, 0.0, 512), BinDef(0.005, 0.0, 1024), BinDef(0.0025, 0.0, 2048),
+              BinDef(0.00125, 0.0, 4096))
+SERVE_GRIDS = (32, 64, 128, 256)
+SERVE_VOLUMES = (64, 96, 128, 160, 192)
+
+
+def serving_mix(num_requests, seed=0, num_meshes=8):
+    """Serving workload: `num_meshes` meshes with 320 to 50k triangles (a
+    jittered level-2 icosphere, a displaced level-3 icosphere, then lat/long
+    spheres and random boxes with log-uniform counts), wall grids of 32^2 to
+    256^2 scan points, bin sets of 512 to 4096 bins spanning 5.12 m, volumes
+    of 64^3 to 192^3 over [-0.5,0.5]^2 x [0.5,1.5]; a request list of 60% mesh
+    requests (half renders, half gradients) and 40% Velten backprojections
+    with uniformly drawn grid, bins, mesh and volume. Measurements (gradient
+    targets, backprojection inputs) are renders of a separate target mesh."""
+    g = rng(seed)
+    meshes = {"m0": jittered_sphere(2, seed + 1), "m1": displaced_sphere(3, seed + 2)}
+    for i in range(2, num_meshes):
+        nf = int(round(math.exp(g.uniform(math.log(320), math.log(50000)))))
+        c = (float(g.uniform(-0.15, 0.15)), float(g.uniform(-0.15, 0.15)),
+             float(g.uniform(0.9, 1.1)))
+        meshes["m%d" % i] = (uv_sphere(nf, seed * 100 + i, center=c) if i % 2 == 0
+                             else random_box(nf, seed * 100 + i, center=c))
+    grids = {"g%d" % r: wall_grid(r)[0] for r in SERVE_GRIDS}
+    target = displaced_sphere(3, seed + 99, center=(0.05, -0.05, 1.0))
+    requests = []
+    for _ in range(num_requests):
+        u = g.uniform()
+        grid = "g%d" % SERVE_GRIDS[g.integers(len(SERVE_GRIDS))]
+        b = int(g.integers(len(SERVE_BINS)))
+        meas = "%s_b%d" % (grid, b)
+        if u < 0.3:
+            requests.append(dict(kind="render", grid=grid, bins=b,
+                                 mesh="m%d" % g.integers(num_meshes)))
+        elif u < 0.6:
+            requests.append(dict(kind="grad", grid=grid, bins=b, target=meas,
+                                 mesh="m%d" % g.integers(num_meshes)))
+        else:
+            res = SERVE_VOLUMES[g.integers(len(SERVE_VOLUMES))]
+            requests.append(dict(kind="backproject", grid=grid, bins=b, target=meas,
+                                 volume=VolumeDef((-0.5, -0.5, 0.5), (0.5, 0.5, 1.5), res)))
+    return dict(meshes={k: (v[0][0], v[1][0], v[2][0]) for k, v in meshes.items()},
+                grids=grids, target=(target[0][0], target[1][0], target[2][0]),
+                requests=requests)

@@ -1,0 +1,410 @@
+"""Request server: continuous batching of render, gradient and backprojection
+requests on one GPU.
+
+Resident state (device memory, kept across requests):
+  * meshes — vertices, faces, albedo and the prepared BVH/face records
+    (``totri_mesh_prepare``), built once at registration;
+  * wall grids — scan points;
+  * measurements — transients [T, S] on a registered grid (backprojection
+    inputs and gradient targets);
+  * visibility masks per (mesh, grid), computed by the first request that
+    needs them and kept in an LRU cache (bins do not change visibility).
+
+Requests are admitted first-come-first-served with a bounded look-ahead
+whenever a stream slot is free and their device memory (outputs, scratch,
+masks still to be computed) fits the HBM budget next to the resident state;
+admitted requests run concurrently on separate CUDA streams, so small requests
+overlap each other and large ones. A request's result is copied to pinned host
+memory on its stream and its future resolves when that copy has completed.
+
+Kinds (``Request.kind``):
+  * "render"      — confocal mesh transient [T, S] (``mesh``, ``grid``, ``bins``);
+  * "grad"        — loss mean((render - target)^2) against measurement
+                    ``target`` and its gradients: (loss, verts_grad [V, 3],
+                    colors_grad [V, 1]);
+  * "backproject" — Velten confocal backprojection of measurement ``target``
+                    into ``volume`` (a VolumeDef): volume [D, H, W].
+"""
+import collections
+import concurrent.futures
+import dataclasses
+import itertools
+import threading
+import time
+import typing
+
+import torch
+
+from . import _lib
+from .totri_cpp import reconstruct as K
+from .types import BinDef, VolumeDef
+
+
+@dataclasses.dataclass
+class Request:
+    kind: str
+    grid: str
+    mesh: typing.Optional[str] = None
+    bins: typing.Optional[BinDef] = None
+    target: typing.Optional[str] = None
+    volume: typing.Optional[VolumeDef] = None
+    # filled in by the server
+    id: int = -1
+    arrival: float = 0.0
+    admitted: float = 0.0
+    done: float = 0.0
+
+
+class Budget:
+    """Byte accounting of the HBM budget: resident bytes plus in-flight bytes."""
+
+    def __init__(self, total):
+        self.total = int(total)
+        self.resident = 0
+        self.inflight = 0
+        self.peak = 0
+
+    def free(self):
+        return self.total - self.resident - self.inflight
+
+    def fits(self, need):
+        return need <= self.free()
+
+    def take(self, need):
+        self.inflight += need
+        self.peak = max(self.peak, self.resident + self.inflight)
+
+    def give(self, need):
+        self.inflight -= need
+
+
+class MaskCache:
+    """LRU cache of visibility masks keyed by (mesh, grid). Entries in use by
+    in-flight requests are pinned; eviction frees the least recently used
+    unpinned entries until the requested bytes fit."""
+
+    Entry = collections.namedtuple("Entry", "buf nbytes ready")
+
+    def __init__(self, budget: Budget):
+        self.budget = budget
+        self.entries = collections.OrderedDict()
+        self.pins = collections.Counter()
+
+    def get(self, key):
+        e = self.entries.get(key)
+        if e is not None:
+            self.entries.move_to_end(key)
+        return e
+
+    def put(self, key, entry):
+        self.entries[key] = entry
+        self.budget.resident += entry.nbytes
+        self.budget.peak = max(self.budget.peak, self.budget.resident + self.budget.inflight)
+
+    def pin(self, key):
+        self.pins[key] += 1
+
+    def unpin(self, key):
+        self.pins[key] -= 1
+        if self.pins[key] <= 0:
+            del self.pins[key]
+
+    def make_room(self, need):
+        """Evicts unpinned entries (LRU first) until `need` bytes fit."""
+        for key in list(self.entries):
+            if self.budget.fits(need):
+                return True
+            if self.pins.get(key):
+                continue
+            e = self.entries.pop(key)
+            self.budget.resident -= e.nbytes
+        return self.budget.fits(need)
+
+
+class _Mesh:
+    def __init__(self, verts, faces, colors, ws):
+        self.verts, self.faces, self.colors, self.ws = verts, faces, colors, ws
+        self.F = faces.shape[1]
+
+
+class Server:
+    """Continuous-batching request server (one GPU, `slots` CUDA streams)."""
+
+    def __init__(self, device=None, hbm_budget=80e9, slots=4, lookahead=8):
+        self.device = torch.device(device or "cuda")
+        self.lib = _lib.load()
+        self.budget = Budget(hbm_budget)
+        self.masks = MaskCache(self.budget)
+        self.meshes, self.grids, self.measurements = {}, {}, {}
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.lookahead = lookahead
+        self.queue = collections.deque()
+        self.inflight = {}  # slot -> (request, future, event, release, result)
+        self.cv = threading.Condition()
+        self.ids = itertools.count()
+        self.thread = None
+        self.running = False
+        self.completed = []
+
+    # -- resident state -----------------------------------------------------
+
+    def _account(self, *tensors):
+        self.budget.resident += sum(t.numel() * t.element_size() for t in tensors)
+
+    def register_mesh(self, name, verts, faces, colors=None):
+        """verts [V, 3], faces [F, 3], colors [V, 1]: copied to the device and
+        prepared (BVH + face records) once."""
+        dev = self.device
+        v = verts.to(dev, torch.float32).reshape(1, -1, 3).contiguous()
+        f = faces.to(dev, torch.int32).reshape(1, -1, 3).contiguous()
+        c = (torch.ones((1, v.shape[1], 1), device=dev) if colors is None
+             else colors.to(dev, torch.float32).reshape(1, v.shape[1], -1)[..., :1].contiguous())
+        n = int(self.lib.totri_mesh_workspace(1, v.shape[1], f.shape[1], 0))
+        ws = torch.empty(max(n, 1), dtype=torch.uint8, device=dev)
+        A = _lib.array
+        _lib.check(self.lib.totri_mesh_prepare(A(v), A(f), A(c), ctypes_ptr(ws), n,
+                                               _lib.stream_of(dev)))
+        torch.cuda.current_stream(dev).synchronize()
+        self._account(v, f, c, ws)
+        self.meshes[name] = _Mesh(v, f, c, ws)
+
+    def register_grid(self, name, scan_points):
+        sp = scan_points.to(self.device, torch.float32).reshape(1, -1, 3).contiguous()
+        self._account(sp)
+        self.grids[name] = sp
+
+    def register_measurement(self, name, transient, grid, bins: BinDef):
+        """transient [T, S] on registered grid `grid`, binned by `bins`."""
+        tr = transient.to(self.device, torch.float32).reshape(1, *transient.shape[-2:])
+        tr = tr.contiguous()
+        if tr.shape[2] != self.grids[grid].shape[1]:
+            raise ValueError("measurement has %d scan points, grid %s has %d"
+                             % (tr.shape[2], grid, self.grids[grid].shape[1]))
+        if tr.shape[1] != bins.num:
+            raise ValueError("measurement has %d bins, its BinDef %d" % (tr.shape[1], bins.num))
+        self._account(tr)
+        self.measurements[name] = (tr, grid, bins)
+
+    # -- requests -----------------------------------------------------------
+
+    def submit(self, req: Request) -> concurrent.futures.Future:
+        self._validate(req)
+        fut = concurrent.futures.Future()
+        with self.cv:
+            req.id = next(self.ids)
+            req.arrival = time.perf_counter()
+            self.queue.append((req, fut))
+            self.cv.notify()
+        return fut
+
+    def _validate(self, r):
+        if r.grid not in self.grids:
+            raise KeyError("unknown grid %r" % r.grid)
+        if r.kind in ("render", "grad"):
+            if r.mesh not in self.meshes:
+                raise KeyError("unknown mesh %r" % r.mesh)
+            if r.bins is None:
+                raise ValueError("render/grad requests need bins")
+        if r.kind in ("grad", "backproject"):
+            if r.target not in self.measurements:
+                raise KeyError("unknown measurement %r" % r.target)
+            tr, grid, bins = self.measurements[r.target]
+            if grid != r.grid:
+                raise ValueError("measurement %r is on grid %r" % (r.target, grid))
+            if r.kind == "grad" and (bins.num, bins.width, bins.offset) != (
+                    r.bins.num, r.bins.width, r.bins.offset):
+                raise ValueError("measurement %r is binned differently from the request"
+                                 % r.target)
+        if r.kind == "backproject" and r.volume is None:
+            raise ValueError("backproject requests need a VolumeDef")
+        if r.kind not in ("render", "grad", "backproject"):
+            raise ValueError("unknown request kind %r" % r.kind)
+
+    def _mask_bytes(self, r):
+        S = self.grids[r.grid].shape[1]
+        return int(self.lib.totri_mesh_mask_bytes(1, self.meshes[r.mesh].F, S))
+
+    def _need(self, r):
+        """Device bytes a request allocates while in flight (outputs, scratch,
+        masks it has to compute)."""
+        S = self.grids[r.grid].shape[1]
+        if r.kind == "backproject":
+            return 4 * int(torch.tensor(r.volume.resolution).prod())
+        m = self.meshes[r.mesh]
+        need = 4 * r.bins.num * S
+        if r.kind == "grad":
+            need = 2 * need + 4 * 4 * m.verts.shape[1]
+        if self.masks.get((r.mesh, r.grid)) is None:
+            need += self._mask_bytes(r)
+        return need
+
+    # -- execution -----------------------------------------------------------
+
+    def _launch(self, r, stream):
+        """Enqueues request r on `stream`; returns (release bytes, host result
+        holder, mask key pinned or None)."""
+        dev = self.device
+        A = _lib.array
+        sp = self.grids[r.grid]
+        S = sp.shape[1]
+        key = None
+        if r.kind in ("render", "grad"):
+            m = self.meshes[r.mesh]
+            key = (r.mesh, r.grid)
+            e = self.masks.get(key)
+            if e is None:
+                nbytes = self._mask_bytes(r)
+                buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+                _lib.check(self.lib.totri_mesh_prepared_visibility(
+                    A(m.verts), A(m.faces), A(m.colors), A(sp), ctypes_ptr(m.ws),
+                    m.ws.numel(), ctypes_ptr(buf), nbytes, _lib.stream_of(dev)))
+                ready = torch.cuda.Event()
+                ready.record(stream)
+                e = MaskCache.Entry(buf, nbytes, ready)
+                self.masks.put(key, e)
+            else:
+                stream.wait_event(e.ready)
+                e.buf.record_stream(stream)
+            self.masks.pin(key)
+            empty = sp[:, :0]
+            bd = r.bins
+            tr = torch.empty((1, bd.num, S), device=dev)
+            _lib.check(self.lib.totri_mesh_prepared_confocal_forward(
+                A(m.verts), A(m.faces), A(m.colors), A(sp), A(empty), A(tr), float(bd.width),
+                float(bd.offset), ctypes_ptr(m.ws), m.ws.numel(), ctypes_ptr(e.buf), e.nbytes,
+                _lib.stream_of(dev)))
+            if r.kind == "render":
+                host = torch.empty(tr.shape[1:], dtype=torch.float32, pin_memory=True)
+                host.copy_(tr[0], non_blocking=True)
+                return host
+            target = self.measurements[r.target][0]
+            target.record_stream(stream)
+            diff = tr - target
+            loss = (diff * diff).mean()
+            tg = diff.mul_(2.0 / diff.numel())
+            vg = torch.empty_like(m.verts)
+            cg = torch.empty_like(m.colors)
+            _lib.check(self.lib.totri_mesh_prepared_confocal_grad_verts(
+                A(m.verts), A(m.faces), A(m.colors), A(sp), A(empty), A(tg), A(vg), A(cg),
+                float(bd.width), float(bd.offset), ctypes_ptr(m.ws), m.ws.numel(),
+                ctypes_ptr(e.buf), e.nbytes, _lib.stream_of(dev)))
+            out = (torch.empty((), dtype=torch.float32, pin_memory=True),
+                   torch.empty(vg.shape[1:], dtype=torch.float32, pin_memory=True),
+                   torch.empty(cg.shape[1:], dtype=torch.float32, pin_memory=True))
+            out[0].copy_(loss, non_blocking=True)
+            out[1].copy_(vg[0], non_blocking=True)
+            out[2].copy_(cg[0], non_blocking=True)
+            return out
+        tr, _, bd = self.measurements[r.target]
+        tr.record_stream(stream)
+        vd = r.volume
+        vol = torch.empty((1,) + tuple(vd.resolution), device=dev)
+        K.backprojection_confocal_velten_forward(tr, sp, sp[:, :0], vol, vd.start, vd.end,
+                                                 bd.width, bd.offset)
+        host = torch.empty(vol.shape[1:], dtype=torch.float32, pin_memory=True)
+        host.copy_(vol[0], non_blocking=True)
+        return host
+
+    def _admit_one(self):
+        """Admits the first of the next `lookahead` queued requests that fits."""
+        free = [i for i in range(len(self.streams)) if i not in self.inflight]
+        if not free or not self.queue:
+            return False
+        cached = sum(e.nbytes for e in self.masks.entries.values())
+        ceiling = self.budget.total - (self.budget.resident - cached)
+        for qi in range(min(self.lookahead, len(self.queue))):
+            r, fut = self.queue[qi]
+            need = self._need(r)
+            if need > ceiling:  # could never fit, even on an idle device
+                del self.queue[qi]
+                fut.set_exception(MemoryError(
+                    "request needs %d bytes; the HBM budget leaves %d next to the resident "
+                    "state" % (need, ceiling)))
+                return True
+            if not self.budget.fits(need) and not self.masks.make_room(need):
+                continue
+            del self.queue[qi]
+            slot = free[0]
+            stream = self.streams[slot]
+            self.budget.take(need)
+            r.admitted = time.perf_counter()
+            try:
+                with torch.cuda.stream(stream):
+                    result = self._launch(r, stream)
+                    ev = torch.cuda.Event()
+                    ev.record(stream)
+            except Exception as exc:  # invalid request data: fail this request only
+                self.budget.give(need)
+                if r.kind in ("render", "grad") and (r.mesh, r.grid) in self.masks.pins:
+                    self.masks.unpin((r.mesh, r.grid))
+                fut.set_exception(exc)
+                return True
+            self.inflight[slot] = (r, fut, ev, need, result)
+            return True
+        return False
+
+    def _reap(self):
+        done = False
+        for slot in list(self.inflight):
+            r, fut, ev, need, result = self.inflight[slot]
+            if not ev.query():
+                continue
+            del self.inflight[slot]
+            self.budget.give(need)
+            if r.kind in ("render", "grad"):
+                self.masks.unpin((r.mesh, r.grid))
+            r.done = time.perf_counter()
+            self.completed.append(r)
+            fut.set_result(result)
+            done = True
+        return done
+
+    def _loop(self):
+        torch.cuda.set_device(self.device)
+        while True:
+            with self.cv:
+                if not self.running and not self.queue and not self.inflight:
+                    return
+                if not self.queue and not self.inflight:
+                    self.cv.wait(timeout=0.05)
+                    continue
+                progressed = self._reap()
+                while self._admit_one():
+                    progressed = True
+            if not progressed:
+                time.sleep(5e-5)
+
+    def start(self):
+        if self.thread is None:
+            self.running = True
+            self.thread = threading.Thread(target=self._loop, daemon=True)
+            self.thread.start()
+        return self
+
+    def stop(self):
+        """Finishes every queued and in-flight request, then stops the loop."""
+        with self.cv:
+            self.running = False
+            self.cv.notify()
+        if self.thread is not None:
+            self.thread.join()
+            self.thread = None
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    def latency_ms(self):
+        """(p50, p99) of completion - arrival over completed requests, in ms."""
+        lat = sorted(1e3 * (r.done - r.arrival) for r in self.completed)
+        if not lat:
+            return None, None
+        pick = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
+        return pick(0.5), pick(0.99)
+
+
+def ctypes_ptr(t):
+    import ctypes
+    return ctypes.c_void_p(t.data_ptr())
