@@ -303,9 +303,15 @@ def batched_metrics(device, count=32, steps=2):
                                          bd.width, bd.offset, 0)
 
     plain()
+    from totri_gb300 import _lib
+    _lib.profile_reset()
+    _lib.profile_enable(True)
     ms_plain = timed(plain, 1)
+    _lib.profile_enable(False)
+    kernels = {k: {"launches": v[0], "ms": v[2]} for k, v in _lib.profile_read().items()}
     torch.cuda.empty_cache()
     return {
+        "kernels_plain_pass": kernels,
         "value": triples / (ms_batched / 1e3), "unit": "triples/s", "ms": ms_batched,
         "plain_calls": {"value": triples / (ms_plain / 1e3), "ms": ms_plain},
         "speedup_vs_plain": ms_plain / ms_batched,

@@ -48,9 +48,10 @@ def _server(meshes, grids, **kw):
         srv.register_mesh(name, v[0], f[0], c[0])
     for name, sp in grids.items():
         srv.register_grid(name, sp)
+    target = scenes.displaced_sphere(3, 35, center=(0.0, 0.05, 1.05))  # not a request mesh
     for g, sp in grids.items():
         for bd, tag in ((BINS, "a"), (BINS2, "b")):
-            meas = _plain_render(meshes["bumpy"], sp, bd)[0]
+            meas = _plain_render(target, sp, bd)[0]
             srv.register_measurement("%s_%s" % (g, tag), meas, g, bd)
     return srv
 

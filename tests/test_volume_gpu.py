@@ -139,7 +139,7 @@ def test_exhaustive_forward_and_adjoint(cuda_lib):
                                        g["end"], float(g["bin"][1]), float(g["bin"][2]))
     assert rel(out.cpu().numpy(), g["transient"]) < 1e-4
     w = torch.randn_like(tr)
-    (tr * w).sum().backward()
+    (tr * w).sum().backward(retain_graph=True)
     adj = oracle.volume_exhaustive_adjoint(w[0].cpu().numpy(), vol.shape[1:], sp[0], lp[0], st,
                                            en, bw, 0.0)
     assert rel(v.grad[0].cpu().numpy(), adj) < 1e-5

@@ -18,7 +18,8 @@ import torch
 from . import _lib
 
 CANDIDATES = {
-    "mesh.visibility.mode": (1, 2),  # 1 per-lane BVH walk, 2 warp-packet walk
+    # 1 per-lane BVH walk, 2 warp-packet walk, 3 per-lane with postponed leaf tests
+    "mesh.visibility.mode": (1, 2, 3),
     "mesh.confocal.splat.ts": (1, 2, 4, 8, 16),
     "mesh.exhaustive.splat.lt": (1, 4, 8, 16, 32),
 }

@@ -112,13 +112,16 @@ class BatchedMeshRenderer:
         self.stream = torch.cuda.Stream(dev)
         self.tiles = {}
         if tune:
+            # Each wave is tuned on a proxy: its median mesh alone (tile choices
+            # depend on bins, wall points and face count, not on the batch size).
             splat = "mesh.exhaustive.splat.lt" if self.exhaustive else "mesh.confocal.splat.ts"
             with torch.cuda.stream(self.stream):
                 for w in self.waves:
-                    cls = autotune.shape_class(B=len(w.members), F=w.faces.shape[1], S=S, T=T,
-                                               L=L)
+                    pos = len(w.members) // 2
+                    cls = autotune.shape_class(F=self.sizes[w.members[pos]][1], S=S, T=T, L=L)
                     self.tiles[w.index] = {
-                        key: autotune.tune(key, lambda: self._forward_calls(w), cls)[0]
+                        key: autotune.tune(key, lambda: self._forward_calls(w, pos), cls,
+                                           reps=1)[0]
                         for key in ("mesh.visibility.mode", splat)}
         self.graph_forward = None
         self.graph_step = None
@@ -154,17 +157,21 @@ class BatchedMeshRenderer:
         lp = self.laser_points[None].expand(n, -1, 3)
         return sp, lp, empty, empty
 
-    def _forward_calls(self, w):
+    def _forward_calls(self, w, only=None):
+        """Forward of wave w (of its mesh at position `only` alone, for tuning)."""
         A = _lib.array
-        self._install_tiles(w)
-        tr = self.transient[:len(w.members)]
-        wall = [A(t) for t in self._wall(w)]
-        if self.exhaustive:
-            st = self.lib.totri_mesh_exhaustive_forward(A(w.verts), A(w.faces), A(w.colors),
-                                                         *wall, A(tr), *self._args())
+        if only is None:
+            self._install_tiles(w)
+            sl = slice(0, len(w.members))
         else:
-            st = self.lib.totri_mesh_confocal_forward(A(w.verts), A(w.faces), A(w.colors),
-                                                      *wall, A(tr), *self._args())
+            sl = slice(only, only + 1)
+        tr = self.transient[:sl.stop - sl.start]
+        wall = [A(t[:sl.stop - sl.start]) for t in self._wall(w)]
+        mesh = (A(w.verts[sl]), A(w.faces[sl]), A(w.colors[sl]))
+        if self.exhaustive:
+            st = self.lib.totri_mesh_exhaustive_forward(*mesh, *wall, A(tr), *self._args())
+        else:
+            st = self.lib.totri_mesh_confocal_forward(*mesh, *wall, A(tr), *self._args())
         _lib.check(st)
 
     def _backward_calls(self, w):

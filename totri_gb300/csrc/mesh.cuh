@@ -10,6 +10,8 @@
 // faces bit for bit.
 #pragma once
 
+#include <climits>
+
 #include "common.cuh"
 
 namespace totri {
@@ -294,6 +296,88 @@ __device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, 
     }
   }
   atomicOr(status, kStatusTraversalCap);
+  return true;
+}
+
+// target_visible with postponed leaf tests (the "while-while" organisation
+// of Aila and Laine, HPG 2009): a lane that reaches a leaf parks it and keeps
+// walking internal nodes until no lane of the warp still walking lacks a
+// parked leaf; the triangle tests, the costliest step of the walk, then run
+// together. The leaves tested, and so the answer, are those of
+// target_visible (any occluder settles the ray; order does not matter).
+__device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
+                                                  const Target& tg, fv3 o, uint32_t* status) {
+  constexpr int kDone = INT_MIN;  // below every leaf code ~k, k < n
+  const int k = tg.k;
+  const fv3 D = xsub3(tg.c, o);
+  const float dist = xlen(D);
+  if (!(dist >= 1e-6f)) return false;
+  const fv3 dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+  const float tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+  const int f = tg.f;
+  float tf;
+  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return false;
+  if (n == 1) return true;
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  int stack[64];
+  int sp = 0;
+  auto pop = [&]() { return sp > 0 ? stack[--sp] : kDone; };
+  int node = 0;      // internal node (>= 0), leaf (~k < 0) or kDone
+  int leaf = kDone;  // parked leaf
+  const int cap = 2 * n + 64;
+  int it = 0;
+  while (node != kDone) {
+    while (node >= 0) {
+      if (++it > cap || node >= n - 1) {  // malformed tree
+        atomicOr(status, kStatusTraversalCap);
+        return true;
+      }
+      const float4* nd = node_at(sc, b, node);
+      const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+      float tn0, tn1;
+      const bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
+      const bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (h0 && h1) {
+        const bool first0 = tn0 <= tn1;
+        if (sp < 64) stack[sp++] = first0 ? c1 : c0;
+        else atomicOr(status, kStatusTraversalCap);
+        node = first0 ? c0 : c1;
+      } else if (h0) {
+        node = c0;
+      } else if (h1) {
+        node = c1;
+      } else {
+        node = pop();
+      }
+      if (node < 0 && node != kDone && leaf == kDone) {
+        leaf = node;
+        node = pop();
+      }
+      if (!__any_sync(__activemask(), leaf == kDone)) break;
+    }
+    while (leaf != kDone) {
+      const int kk = ~leaf;
+      if (kk != k) {
+        if (kk < 0 || kk >= n) {
+          atomicOr(status, kStatusTraversalCap);
+        } else {
+          const float4* q = tri_at(sc, b, kk);
+          const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+          float tq;
+          if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
+              (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
+            return false;
+        }
+      }
+      leaf = kDone;
+      if (node < 0 && node != kDone) {
+        leaf = node;
+        node = pop();
+      }
+    }
+  }
   return true;
 }
 

@@ -27,14 +27,17 @@ namespace {
 
 // One warp per (wall point, 32 Morton-consecutive faces): the 32 rays share
 // their origin and end on a compact patch of the surface, so they walk
-// largely the same BVH nodes. kVisRay lets each lane walk alone
-// (target_visible; the default), kVisPacket walks them as one warp packet
-// (packet_visible; about twice the node visits on the 20,480-face sphere
-// seen from a 64x64 wall, so only the tuner picks it), kVisBrute tests every
-// face; all three give the same bits.
+// largely the same BVH nodes. kVisRayPostponed (the default) lets each lane
+// walk alone with its triangle tests postponed until the warp runs them
+// together (target_visible_pp; 22.8 ms against 27.0 ms for kVisRay, the plain
+// per-lane walk target_visible, on the 20,480-face sphere seen from a 64x64
+// wall), kVisPacket walks the 32 rays as one warp packet (packet_visible;
+// about twice the node visits there), kVisBrute tests every face; all four
+// give the same bits.
 constexpr int kVisBrute = 0;
 constexpr int kVisRay = 1;
 constexpr int kVisPacket = 2;
+constexpr int kVisRayPostponed = 3;
 
 template <int kMode>
 __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
@@ -57,6 +60,8 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
       if (k < n) tg = load_target(sc, b, k);
       vis = packet_visible(sc, b, n, k < n, tg, o, sc.status);
     }
+  } else if (kMode == kVisRayPostponed) {
+    if (k < n) vis = target_visible_pp(sc, b, n, load_target(sc, b, k), o, sc.status);
   } else if (k < n) {
     int cache = -1;
     vis = target_visible<kMode == kVisBrute>(sc, b, n, load_target(sc, b, k), o, cache,
@@ -195,7 +200,7 @@ __device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c,
 __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f so, int has_origin,
                                                    const float* __restrict__ tgrad, int T, int S,
                                                    float bw, float bo, GradOut out) {
-  extern __shared__ uint32_t mcol[];  // [S] mask words of this 32-face chunk
+  extern __shared__ uint32_t mcol[];  // [slice] mask words of this 32-face chunk
   const int b = blockIdx.y;
   const int ch = blockIdx.x;
   const int n = sc.meta[b].n;
@@ -204,7 +209,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
   const int s0 = (int)((int64_t)S * blockIdx.z / gridDim.z);
   const int s1 = (int)((int64_t)S * (blockIdx.z + 1) / gridDim.z);
   for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x)
-    mcol[s] = sc.mask[((size_t)b * sc.P + s) * sc.nch + ch];
+    mcol[s - s0] = sc.mask[((size_t)b * sc.P + s) * sc.nch + ch];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const float* tgb = tgrad + (size_t)b * T * S;
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
     fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
     float accm = 0.f;
     for (int s = s0 + lane; s < s1; s += 32) {
-      if (!((mcol[s] >> j) & 1u)) continue;
+      if (!((mcol[s - s0] >> j) & 1u)) continue;
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       float od = 0.f;
       if (has_origin)
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
       fv3 dv[3];
       float dm;
       if (!pair_grad_confocal(q, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) continue;
-      for (int kk = 0; kk < 3; ++kk) acc[q.perm[kk]] = acc[q.perm[kk]] + dv[kk];
+      add_permuted(acc, dv, q.perm);
       accm += dm;
     }
     scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
@@ -265,12 +270,16 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
   if (brute) {
     TOTRI_KERNEL("mesh visibility brute", stream,
                  visibility_kernel<kVisBrute><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
+  } else if (tune::get("mesh.visibility.mode") == kVisRay) {
+    TOTRI_KERNEL("mesh visibility", stream,
+                 visibility_kernel<kVisRay><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
   } else if (tune::get("mesh.visibility.mode") == kVisPacket) {
     TOTRI_KERNEL("mesh visibility", stream,
                  visibility_kernel<kVisPacket><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
   } else {
     TOTRI_KERNEL("mesh visibility", stream,
-                 visibility_kernel<kVisRay><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
+                 visibility_kernel<kVisRayPostponed><<<blocks, 256, 0, stream>>>(sc, pts, P,
+                                                                                  row0));
   }
   return TOTRI_OK;
 }
@@ -324,15 +333,16 @@ int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, i
 int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,
                          const float* tgrad, int T, int S, float bw, float bo,
                          const GradOut& out, cudaStream_t stream) {
-  const size_t smem = sizeof(uint32_t) * (size_t)S;
-  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many scan points for one tile");
+  constexpr int kMaxSlice = 16384;  // 64 KB of mask words per CTA
+  const int split =
+      tune::grad_split("mesh.confocal.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
+  const size_t smem = sizeof(uint32_t) * (size_t)ceil_div(S, split);
   static int configured = 0;
   if (smem > 48 * 1024 && configured < (int)smem) {
     TOTRI_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
     configured = (int)smem;
   }
-  const int split = tune::grad_split("mesh.confocal.grad.split", (int64_t)sc.nch * sc.B, S);
   const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh confocal grad", stream,
                grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, tgrad, T, S, bw,

@@ -123,6 +123,90 @@ __global__ void __launch_bounds__(256) exh_splat_kernel(Scene sc, View3f sp, Vie
   }
 }
 
+// Forward with the visible triples compacted first (tuning option). Visibility is separable,
+// so for the CTA's scan point s and each of its LT lasers the visible faces of
+// a 32-face chunk are one AND of two mask words. Each warp walks its chunks,
+// appends the visible (face, laser) pairs to a per-warp queue in shared memory
+// and evaluates them 32 at a time, one per lane: every lane does useful work
+// instead of most lanes waiting on mask tests that fail.
+constexpr int kExhQueue = 64;
+
+template <int LT>
+__global__ void __launch_bounds__(256) exh_splat_compact_kernel(Scene sc, View3f sp, View3f lp,
+                                                                Origins org, int S, int L,
+                                                                float* __restrict__ out, int T,
+                                                                float bw, float bo) {
+  extern __shared__ float hist[];  // [T][LT]
+  __shared__ float lpt[LT][4];     // laser point, laser-origin term
+  __shared__ int queue[8][kExhQueue];
+  const int b = blockIdx.z;
+  const int s = blockIdx.x;
+  const int l0 = blockIdx.y * LT;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < T * LT; i += blockDim.x) hist[i] = 0.f;
+  const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+  if (threadIdx.x < LT && l0 + (int)threadIdx.x < L) {
+    const int l = l0 + threadIdx.x;
+    const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
+    lpt[threadIdx.x][0] = q.x;
+    lpt[threadIdx.x][1] = q.y;
+    lpt[threadIdx.x][2] = q.z;
+    lpt[threadIdx.x][3] = origin_term(org, b, s, l, p, q);
+  }
+  __syncthreads();
+  const int n = sc.meta[b].n;
+  const int nchu = (n + 31) >> 5;
+  const uint32_t* ms = sc.mask + ((size_t)b * sc.P + s) * sc.nch;
+  const uint32_t* ml = sc.mask + ((size_t)b * sc.P + S) * sc.nch;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  const int lts = min(LT, L - l0);
+  const uint32_t below = (1u << lane) - 1u;
+  int* qw = queue[warp];
+  int cnt = 0;  // warp-uniform
+  auto run = [&](int e) {
+    const int k = e >> 5, l = e & 31;
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 q = mkv(lpt[l][0], lpt[l][1], lpt[l][2]);
+    ExhPair ep;
+    exh_pair(s0r, s1r, s2r, p, q, lpt[l][3], bw, bo, ep);
+    const float alpha = alpha_exhaustive(ep, mkv(s3r.x, s3r.y, s3r.z), p, q, s0r.w);
+    if (!(alpha > 0.f)) return;
+    const Hist<LT> h{hist, l, T};
+    splat_tent(h, ep.c, ep.bin, alpha);
+  };
+  for (int ch = warp; ch < nchu; ch += 8) {
+    const uint32_t msw = __ldg(ms + ch);
+    if (msw == 0u) continue;
+    const uint32_t lw =
+        lane < lts ? (__ldg(ml + (size_t)(l0 + lane) * sc.nch + ch) & msw) : 0u;
+    for (int l = 0; l < lts; ++l) {
+      const uint32_t bits = __shfl_sync(0xffffffffu, lw, l);
+      if (bits == 0u) continue;
+      if ((bits >> lane) & 1u) qw[cnt + __popc(bits & below)] = ((ch * 32 + lane) << 5) | l;
+      cnt += __popc(bits);
+      if (cnt >= 32) {
+        __syncwarp();
+        const int e = qw[lane];
+        __syncwarp();
+        if (lane < cnt - 32) qw[lane] = qw[32 + lane];
+        cnt -= 32;
+        __syncwarp();
+        run(e);
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < cnt) run(qw[lane]);
+  __syncthreads();
+  // rows out[b][t][s][l0 .. l0+LT)
+  float* ob = out + (((size_t)b * T) * S + s) * L + l0;
+  for (int i = threadIdx.x; i < T * LT; i += blockDim.x) {
+    const int t = i / LT, c = i - t * LT;
+    if (l0 + c < L) ob[(size_t)t * S * L + c] = hist[i];
+  }
+}
+
 // Gradient of one visible triple w.r.t. the sorted vertices and the albedo
 // (mesh_exhaustive_grad_verts_optix.cu:336-412, AlphaExhaustiveGradVerts
 // mesh_common.h:549-630).
@@ -209,10 +293,101 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
         float dm;
         if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
           continue;
-        for (int kk = 0; kk < 3; ++kk) acc[e.perm[kk]] = acc[e.perm[kk]] + dv[kk];
+        add_permuted(acc, dv, e.perm);
         accm += dm;
       }
     }
+    scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
+  }
+}
+
+// Gradient with the visible (scan point, laser) pairs of each face compacted:
+// the CTA holds its 32 faces' scan-mask words for a slice of scan points and,
+// per face, the set of lasers that see it (transposed from the laser rows by
+// warp ballots). A warp walks one face at a time, queues its visible
+// (s, l) pairs and evaluates them 32 at a time, one per lane; the face's
+// gradient stays in registers and is reduced and scattered once per CTA.
+__global__ void __launch_bounds__(256) exh_grad_compact_kernel(
+    Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
+    int T, float bw, float bo, GradOut out) {
+  extern __shared__ uint32_t words[];  // [slice] scan words | [32][LW] laser sets
+  __shared__ int qs[8][kExhQueue], ql[8][kExhQueue];
+  const int b = blockIdx.y;
+  const int ch = blockIdx.x;
+  const int n = sc.meta[b].n;
+  if (ch * 32 >= n) return;
+  const int s0 = (int)((int64_t)S * blockIdx.z / gridDim.z);
+  const int s1 = (int)((int64_t)S * (blockIdx.z + 1) / gridDim.z);
+  const int ns = s1 - s0;
+  const int LW = (L + 31) >> 5;
+  uint32_t* mcs = words;
+  uint32_t* lvis = words + ns;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t* mrow = sc.mask + (size_t)b * sc.P * sc.nch + ch;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) mcs[i] = mrow[(size_t)(s0 + i) * sc.nch];
+  for (int wl = warp; wl < LW; wl += 8) {
+    const int l = wl * 32 + lane;
+    const uint32_t m = l < L ? mrow[(size_t)(S + l) * sc.nch] : 0u;
+    for (int j = 0; j < 32; ++j) {
+      const uint32_t bal = __ballot_sync(0xffffffffu, (m >> j) & 1u);
+      if (lane == 0) lvis[j * LW + wl] = bal;
+    }
+  }
+  __syncthreads();
+  const float* tgb = tgrad + (size_t)b * T * S * L;
+  const int64_t stride = (int64_t)S * L;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  const uint32_t below = (1u << lane) - 1u;
+  for (int j = warp; j < 32; j += 8) {
+    const int k = ch * 32 + j;
+    if (k >= n) break;
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
+    fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
+    float accm = 0.f;
+    auto run = [&](int s, int l) {
+      const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+      const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
+      ExhPair e;
+      exh_pair(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, e);
+      fv3 dv[3];
+      float dm;
+      if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
+        return;
+      add_permuted(acc, dv, e.perm);
+      accm += dm;
+    };
+    const uint32_t* lv = lvis + j * LW;
+    int cnt = 0;  // warp-uniform
+    for (int si = 0; si < ns; ++si) {
+      if (!((mcs[si] >> j) & 1u)) continue;
+      for (int wl = 0; wl < LW; ++wl) {
+        const uint32_t bits = lv[wl];
+        if (bits == 0u) continue;
+        if ((bits >> lane) & 1u) {
+          const int at = cnt + __popc(bits & below);
+          qs[warp][at] = s0 + si;
+          ql[warp][at] = wl * 32 + lane;
+        }
+        cnt += __popc(bits);
+        if (cnt >= 32) {
+          __syncwarp();
+          const int es = qs[warp][lane], el = ql[warp][lane];
+          __syncwarp();
+          if (lane < cnt - 32) {
+            qs[warp][lane] = qs[warp][32 + lane];
+            ql[warp][lane] = ql[warp][32 + lane];
+          }
+          cnt -= 32;
+          __syncwarp();
+          run(es, el);
+        }
+      }
+    }
+    __syncwarp();
+    if (lane < cnt) run(qs[warp][lane], ql[warp][lane]);
+    __syncwarp();
     scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
   }
 }
@@ -222,16 +397,31 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
                             const Origins& org, int S, int L, float* out, int T, float bw,
                             float bo, cudaStream_t stream) {
   const size_t smem = sizeof(float) * (size_t)T * LT;
+  const dim3 grid((unsigned)S, (unsigned)ceil_div(L, LT), (unsigned)sc.B);
+  // Per-thread mask tests by default: on the 32-mesh batch (2048 bins, 64x64
+  // detector x 16x16 laser points) they took 4.4 s against 4.9 s for the
+  // compacted variant, which "mesh.exhaustive.splat.mode" = 1 selects.
+  if (tune::get("mesh.exhaustive.splat.mode") != 1) {
+    static int configured = 0;
+    if (smem > 48 * 1024 && configured < (int)smem) {
+      TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured = (int)smem;
+    }
+    TOTRI_KERNEL("mesh exhaustive splat", stream,
+                 exh_splat_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, out, T,
+                                                                   bw, bo));
+    return TOTRI_OK;
+  }
   static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT>,
+  if (smem > 32 * 1024 && configured < (int)smem) {  // 16 KB of static shared memory besides
+    TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_compact_kernel<LT>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = (int)smem;
   }
-  const dim3 grid((unsigned)S, (unsigned)ceil_div(L, LT), (unsigned)sc.B);
   TOTRI_KERNEL("mesh exhaustive splat", stream,
-               exh_splat_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, out, T, bw,
-                                                                 bo));
+               exh_splat_compact_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L,
+                                                                         out, T, bw, bo));
   return TOTRI_OK;
 }
 
@@ -264,20 +454,40 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
 int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                            const Origins& org, int S, int L, const float* tgrad, int T, float bw,
                            float bo, const GradOut& out, cudaStream_t stream) {
-  const size_t smem = sizeof(uint32_t) * (size_t)(S + L);
-  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points for one tile");
+  constexpr int kMaxSlice = 16384;
+  const int split =
+      tune::grad_split("mesh.exhaustive.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
+  const int64_t slice = ceil_div(S, split);
+  // Compacted by default (14.7 s against 17.7 s for per-lane mask tests on the
+  // 32-mesh batch); "mesh.exhaustive.grad.mode" = 1 selects the latter.
+  if (tune::get("mesh.exhaustive.grad.mode") == 1) {
+    const size_t smem = sizeof(uint32_t) * (size_t)(S + L);
+    if (smem > 200 * 1024)
+      return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points for one tile");
+    static int configured = 0;
+    if (smem > 48 * 1024 && configured < (int)smem) {
+      TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured = (int)smem;
+    }
+    const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
+    TOTRI_KERNEL("mesh exhaustive grad", stream,
+                 exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T,
+                                                              bw, bo, out));
+    return TOTRI_OK;
+  }
+  const size_t smem = sizeof(uint32_t) * (size_t)(slice + 32 * ceil_div(L, 32));
+  if (smem > 180 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many laser points for one tile");
   static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
+  if (smem > 32 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_compact_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = (int)smem;
   }
-  const int split =
-      tune::grad_split("mesh.exhaustive.grad.split", (int64_t)sc.nch * sc.B, S);
   const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh exhaustive grad", stream,
-               exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T, bw,
-                                                            bo, out));
+               exh_grad_compact_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad,
+                                                                    T, bw, bo, out));
   return TOTRI_OK;
 }
 

@@ -190,6 +190,16 @@ __device__ __forceinline__ float warp_sum(float x) {
 // Reduces one face's gradient over the warp and adds it to its vertices
 // (mesh_confocal_grad_verts_optix.cu:316-332; 1/3 of the albedo gradient
 // goes to channel 0 of each vertex).
+// acc[perm[k]] += dv[k] for a permutation perm of {0, 1, 2}, with selects
+// instead of a dynamically indexed array (which would live in local memory).
+__device__ __forceinline__ void add_permuted(fv3 acc[3], const fv3 dv[3], const int perm[3]) {
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const fv3 v = perm[0] == m ? dv[0] : (perm[1] == m ? dv[1] : dv[2]);
+    acc[m] = acc[m] + v;
+  }
+}
+
 __device__ __forceinline__ void scatter_face_grad(const GradOut& out, int b, float4 s1r, float4 s2r,
                                                   float4 s3r, fv3 acc[3], float accm,
                                                   uint32_t* status) {

@@ -50,6 +50,11 @@ void begin(const char* name, cudaStream_t stream, cudaEvent_t* start) {
   g_totals[name].launches += 1;
   *start = nullptr;
   if (!enabled()) return;
+  // launches recorded into a CUDA graph are not timed (the events would
+  // become graph nodes)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return;
   cudaEvent_t e = take_event();
   if (e && cudaEventRecord(e, stream) == cudaSuccess) *start = e;
 }

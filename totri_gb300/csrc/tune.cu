@@ -32,14 +32,17 @@ int sm_count() {
   return n;
 }
 
-int grad_split(const char* key, int64_t ctas, int S) {
-  const int most = S >= 64 ? S / 64 : 1;
-  const int want = get(key);
-  if (want > 0) return want < most ? want : most;
-  if (ctas <= 0) return 1;
-  const int64_t target = (int64_t)sm_count() * 8;
-  const int64_t split = (target + ctas - 1) / ctas;
-  return (int)(split < most ? split : most);
+int grad_split(const char* key, int64_t ctas, int S, int max_slice) {
+  const int least = (int)((S + (int64_t)max_slice - 1) / max_slice);
+  int most = S >= 64 ? S / 64 : 1;
+  if (most < least) most = least;
+  int split = get(key);
+  if (split <= 0) {
+    const int64_t target = (int64_t)sm_count() * 8;
+    split = ctas > 0 ? (int)((target + ctas - 1) / ctas) : 1;
+  }
+  if (split > most) split = most;
+  return split < least ? least : split;
 }
 
 }  // namespace tune

@@ -12,7 +12,8 @@ namespace tune {
 int get(const char* key);  // 0 when unset
 int sm_count();            // multiprocessors of the current device
 // Slices of the scan-point loop for a gradient grid of `ctas` CTAs: enough to
-// give every SM several CTAs, at most one per 64 points (tuned value first).
-int grad_split(const char* key, int64_t ctas, int S);
+// give every SM several CTAs, at most one per 64 points (tuned value first),
+// and never fewer than make each slice at most `max_slice` points long.
+int grad_split(const char* key, int64_t ctas, int S, int max_slice);
 }  // namespace tune
 }  // namespace totri

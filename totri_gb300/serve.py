@@ -131,7 +131,10 @@ class Server:
     """Continuous-batching request server (one GPU, `slots` CUDA streams)."""
 
     def __init__(self, device=None, hbm_budget=80e9, slots=4, lookahead=8):
-        self.device = torch.device(device or "cuda")
+        device = torch.device(device or "cuda")
+        if device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
         self.lib = _lib.load()
         self.budget = Budget(hbm_budget)
         self.masks = MaskCache(self.budget)
@@ -191,6 +194,8 @@ class Server:
         self._validate(req)
         fut = concurrent.futures.Future()
         with self.cv:
+            if self.thread is not None and not self.thread.is_alive():
+                raise RuntimeError("request server is not running")
             req.id = next(self.ids)
             req.arrival = time.perf_counter()
             self.queue.append((req, fut))
@@ -360,6 +365,21 @@ class Server:
         return done
 
     def _loop(self):
+        try:
+            self._serve()
+        except BaseException as exc:  # the loop died: fail everything still waiting
+            with self.cv:
+                pending = [fut for _, fut in self.queue]
+                pending += [entry[1] for entry in self.inflight.values()]
+                self.queue.clear()
+                self.inflight.clear()
+                self.running = False
+            for fut in pending:
+                if not fut.done():
+                    fut.set_exception(RuntimeError("request server stopped: %r" % (exc,)))
+            raise
+
+    def _serve(self):
         torch.cuda.set_device(self.device)
         while True:
             with self.cv:
