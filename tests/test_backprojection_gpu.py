@@ -100,3 +100,57 @@ def test_velten_adjoint_full_size(cuda_lib):
     ref = oracle.bp_confocal_velten(xs[0].cpu().numpy(), sp[0, sub].cpu().numpy(), None,
                                     vd.resolution, vd.start, vd.end, bd.width, bd.offset)
     assert rel(v[0].cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("offset,origin", [(0.0, False), (0.137, True)])
+def test_velten_bins_exact(cuda_lib, offset, origin):
+    """Bin decisions bit for bit: with transient[t, s] = t + 1 every voxel sums
+    its scan points' bins as integers (exact in FP32 below 2^24), so one bin
+    taken differently from the oracle changes a voxel by exactly 1. Covers the
+    filtered fast path and its exact fallback, forward and adjoint."""
+    g = np.random.default_rng(21)
+    T, res = 700, (40, 36, 44)
+    sp = scenes.wall_grid(24)[0].numpy()
+    S = sp.shape[0]
+    tr = np.broadcast_to((np.arange(T, dtype=np.float32) + 1)[:, None], (T, S)).copy()
+    so = (sp + g.uniform(-0.3, 0.3, sp.shape).astype(np.float32)) if origin else None
+    st, en, bw = (-0.5, -0.4, 0.6), (0.45, 0.5, 1.4), 0.0043
+    ref = oracle.bp_confocal_velten(tr, sp, so, res, st, en, bw, offset)
+    vol = torch.empty((1,) + res, device="cuda")
+    so_t = torch.from_numpy(so)[None].cuda() if origin else torch.empty((1, 0, 3), device="cuda")
+    K.backprojection_confocal_velten_forward(torch.from_numpy(tr)[None].cuda(),
+                                             torch.from_numpy(sp)[None].cuda(), so_t, vol, st,
+                                             en, bw, offset)
+    assert np.array_equal(vol[0].double().cpu().numpy(), ref)
+    # adjoint: a one-voxel volume of value 1 gives 1 exactly at its bin for every scan point
+    one = np.zeros(res, np.float64)
+    one[17, 5, 30] = 1.0
+    adj_ref = oracle.bp_confocal_velten_adjoint(one, sp, so, T, st, en, bw, offset)
+    adj = torch.empty((1, T, S), device="cuda")
+    K.backprojection_confocal_velten_adjoint(torch.from_numpy(one.astype(np.float32))[None].cuda(),
+                                             torch.from_numpy(sp)[None].cuda(), so_t, adj, st, en,
+                                             bw, offset)
+    assert np.array_equal(adj[0].double().cpu().numpy(), adj_ref)
+
+
+def test_velten_tiled_equals_untiled(cuda_lib):
+    """The shared-memory tiled Velten kernel sums the same values in the same
+    order as the one-voxel-per-thread kernel: identical volumes, including a
+    grid that is not a multiple of the 8x8x4 voxel block and a scan whose
+    bin windows overflow the staged rows."""
+    from totri_gb300 import autotune
+    g = np.random.default_rng(5)
+    for res, S, T, bw in (((37, 29, 50), 300, 900, 0.004), ((16, 16, 16), 1000, 256, 0.05)):
+        tr = torch.from_numpy(g.random((1, T, S), dtype=np.float32)).cuda()
+        sp = torch.from_numpy(np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S),
+                                        np.zeros(S)], -1).astype(np.float32))[None].cuda()
+        out = []
+        for mode in (0, 1):
+            autotune.set_tile("backprojection.velten.mode", mode)
+            v = torch.empty((1,) + res, device="cuda")
+            K.backprojection_confocal_velten_forward(tr, sp, torch.empty((1, 0, 3), device="cuda"),
+                                                     v, (-0.5, -0.4, 0.5), (0.5, 0.45, 1.5), bw,
+                                                     0.01)
+            out.append(v)
+        autotune.set_tile("backprojection.velten.mode", 0)
+        assert torch.equal(out[0], out[1])

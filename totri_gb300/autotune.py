@@ -19,7 +19,10 @@ from . import _lib
 
 CANDIDATES = {
     # 1 per-lane BVH walk, 2 warp-packet walk, 3 per-lane with postponed leaf tests
-    "mesh.visibility.mode": (1, 2, 3),
+    # (point-major warps), 4 postponed leaf tests with face-major warps over
+    # Morton-ordered wall-point patches (the built-in choice), 5 the same warps
+    # walking as one packet
+    "mesh.visibility.mode": (3, 4, 5),
     "mesh.confocal.splat.ts": (1, 2, 4, 8, 16),
     "mesh.exhaustive.splat.lt": (1, 4, 8, 16, 32),
 }

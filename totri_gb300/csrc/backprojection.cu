@@ -7,9 +7,13 @@
 // wall-to-origin distances) in shared memory in tiles, so each scan point is
 // read once per CTA rather than once per voxel. The adjoint owns a tile of
 // scan points and keeps their transient columns in shared memory.
+#include <cmath>
 #include <string>
 
+#include <climits>
+
 #include "capi_common.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace bp {
@@ -38,6 +42,44 @@ __device__ __forceinline__ int nearest_bin(float dist, float bw, float bo) {
   return (int)b;
 }
 
+// Velten bins with a filtered fast path. The decision is nearest_bin(od2 + 2
+// |q - p|) with one IEEE rounding per operation. The fast path evaluates the
+// same expression with fused multiply-adds, the hardware reciprocal square
+// root (2 ulp) and a precomputed 1/bw; against the exact chain its bin
+// coordinate c = (dist - bo)/bw + 1/2 deviates by at most about
+// 14 u (dist + |bo|)/bw + 5 u |c| (u = 2^-24: 3 u from the sum of squares,
+// 6.5 u from the root, one rounding per remaining operation). Where c lies
+// farther than twice that from an integer both floors are equal and the fast
+// bin is returned; otherwise (and for NaN or infinite c) the exact chain runs,
+// so the bins are those of the exact chain everywhere.
+struct FastBin {
+  float inv_bw, nbo, k1, k2;
+};
+
+inline FastBin make_fast_bin(float bw, float bo) {
+  const float u = 5.9604645e-8f;  // 2^-24
+  FastBin f;
+  f.inv_bw = 1.f / bw;
+  f.nbo = -bo * f.inv_bw;
+  const bool ok = bw > 0.f && std::isfinite(f.inv_bw) && std::isfinite(f.nbo);
+  f.k1 = ok ? 32.f * u * f.inv_bw : INFINITY;
+  f.k2 = ok ? 32.f * u * std::fabs(bo) * f.inv_bw + 1e-6f : INFINITY;
+  return f;
+}
+
+__device__ __forceinline__ int velten_bin(fv3 q, float od2, fv3 p, float bw, float bo,
+                                          const FastBin& f) {
+  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float dist = fmaf(2.f, d2 * rsqrtf(d2), od2);
+  const float c = fmaf(dist, f.inv_bw, f.nbo) + 0.5f;
+  const float t = floorf(c);
+  const float fr = c - t;
+  const float m = fmaf(f.k1, dist, f.k2) + 1e-6f * fabsf(c);
+  if (fr > m && fr < 1.f - m && fabsf(t) < 1.0e9f) return (int)t;
+  return nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, p)))), bw, bo);
+}
+
 struct Pts3 {  // [B, n, 3] with strides
   const float* p;
   int64_t sb, sn, sc;
@@ -51,7 +93,7 @@ constexpr int kTile = 512;
 
 __global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int T, int S,
                                                               Pts3 sp, Pts3 so, int has_origin,
-                                                              float bw, float bo,
+                                                              float bw, float bo, FastBin fb,
                                                               const float* __restrict__ tr,
                                                               float* __restrict__ vol) {
   __shared__ float4 pts[kTile];  // scan point xyz, 2 * |scan - origin|
@@ -73,8 +115,7 @@ __global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int
       const int cnt = min(kTile, S - s0);
       for (int j = 0; j < cnt; ++j) {
         const float4 q = pts[j];
-        const float sv = xlen(xsub3(mkv(q.x, q.y, q.z), p));
-        const int t = nearest_bin(xadd(q.w, xmul(2.f, sv)), bw, bo);
+        const int t = velten_bin(mkv(q.x, q.y, q.z), q.w, p, bw, bo, fb);
         if (t >= 0 && t < T) value += __ldg(trb + (size_t)t * S + s0 + j);
       }
     }
@@ -82,11 +123,100 @@ __global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int
   if (v < nv) vol[(size_t)b * nv + v] = value;
 }
 
+// Tiled Velten confocal: one CTA per 8x8x4 block of voxels, scan points in
+// tiles of 32. Per tile, warp 0 bounds the bins the block can reach from each
+// point (distance from the point to the block's box, one bin of margin each
+// side) and the CTA stages the union of those rows of the tile's 32 transient
+// columns in shared memory with coalesced 128-byte row reads (row stride 33,
+// so lanes reading different bins of one column hit different banks). Voxels
+// then read their bin from shared memory; a bin outside the staged rows (or a
+// tile whose rows exceed kWinRows) is read from global memory, so the window
+// only affects speed. The sum runs over the scan points in the same order as
+// velten_confocal_kernel, so the two give identical volumes.
+constexpr int kBX = 8, kBY = 8, kBZ = 4, kST = 32, kWinRows = 256;
+
+__global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
+    Grid g, int b, int T, int S, Pts3 sp, Pts3 so, int has_origin, float bw, float bo,
+    FastBin fb, const float* __restrict__ tr, float* __restrict__ vol) {
+  __shared__ float win[kWinRows * (kST + 1)];
+  __shared__ float4 pts[kST];
+  __shared__ int span[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * kBX, y0 = blockIdx.y * kBY, z0 = blockIdx.z * kBZ;
+  const int x = x0 + (threadIdx.x & 7), y = y0 + ((threadIdx.x >> 3) & 7),
+            z = z0 + (threadIdx.x >> 6);
+  const bool inside = x < g.W && y < g.H && z < g.D;
+  const fv3 p = voxel_point(g, min(x, g.W - 1), min(y, g.H - 1), min(z, g.D - 1));
+  // the block's box: voxel coordinates are monotone in the index
+  const fv3 ca = voxel_point(g, x0, y0, z0);
+  const fv3 cb = voxel_point(g, min(x0 + kBX, g.W) - 1, min(y0 + kBY, g.H) - 1,
+                             min(z0 + kBZ, g.D) - 1);
+  const fv3 lo = mkv(fminf(ca.x, cb.x), fminf(ca.y, cb.y), fminf(ca.z, cb.z));
+  const fv3 hi = mkv(fmaxf(ca.x, cb.x), fmaxf(ca.y, cb.y), fmaxf(ca.z, cb.z));
+  const float* trb = tr + (size_t)b * T * S;
+  float value = 0.f;
+  for (int s0 = 0; s0 < S; s0 += kST) {
+    const int cnt = min(kST, S - s0);
+    __syncthreads();  // the previous tile is consumed
+    if (warp == 0) {
+      int tlo = INT_MAX, thi = INT_MIN;
+      if (lane < cnt) {
+        const fv3 q = sp.at(b, s0 + lane);
+        const float od2 = xmul(2.f, has_origin ? xlen(xsub3(q, so.at(b, s0 + lane))) : 0.f);
+        pts[lane] = make_float4(q.x, q.y, q.z, od2);
+        const float ex = fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.f);
+        const float ey = fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.f);
+        const float ez = fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.f);
+        const float fx = fmaxf(fabsf(lo.x - q.x), fabsf(hi.x - q.x));
+        const float fy = fmaxf(fabsf(lo.y - q.y), fabsf(hi.y - q.y));
+        const float fz = fmaxf(fabsf(lo.z - q.z), fabsf(hi.z - q.z));
+        const float cmin = (od2 + 2.f * sqrtf(ex * ex + ey * ey + ez * ez) - bo) / bw + 0.5f;
+        const float cmax = (od2 + 2.f * sqrtf(fx * fx + fy * fy + fz * fz) - bo) / bw + 0.5f;
+        if (cmin == cmin && cmax == cmax && cmax >= -1.f && cmin <= (float)T + 1.f) {
+          tlo = max((int)floorf(fmaxf(cmin, -2.f)) - 1, 0);
+          thi = min((int)floorf(fminf(cmax, (float)T + 2.f)) + 1, T - 1);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        tlo = min(tlo, __shfl_xor_sync(0xffffffffu, tlo, o));
+        thi = max(thi, __shfl_xor_sync(0xffffffffu, thi, o));
+      }
+      if (lane == 0) {
+        span[0] = tlo;
+        span[1] = thi;
+      }
+    }
+    __syncthreads();
+    // an empty window leaves tlo = INT_MAX, thi = INT_MIN: no rows (the
+    // difference must not be formed, it overflows)
+    const int tlo = span[0], thi = span[1];
+    const int rows = (tlo >= 0 && thi < T && thi >= tlo) ? thi - tlo + 1 : 0;
+    const bool staged = rows > 0 && rows <= kWinRows;
+    if (staged)
+      for (int i = threadIdx.x; i < rows * kST; i += blockDim.x) {
+        const int r = i >> 5, c = i & 31;
+        win[r * (kST + 1) + c] = c < cnt ? __ldg(trb + (size_t)(tlo + r) * S + s0 + c) : 0.f;
+      }
+    __syncthreads();
+    if (inside) {
+      for (int j = 0; j < cnt; ++j) {
+        const float4 q = pts[j];
+        const int t = velten_bin(mkv(q.x, q.y, q.z), q.w, p, bw, bo, fb);
+        if (t < 0 || t >= T) continue;
+        const int r = t - tlo;
+        value += (staged && r >= 0 && r < rows) ? win[r * (kST + 1) + j]
+                                                : __ldg(trb + (size_t)t * S + s0 + j);
+      }
+    }
+  }
+  if (inside) vol[(size_t)b * g.D * g.H * g.W + ((size_t)z * g.H + y) * g.W + x] = value;
+}
+
 // Adjoint: transient [T, S] tile of TS scan points in shared memory, all voxels.
 constexpr int kTS = 8;
 __global__ void __launch_bounds__(256) velten_adjoint_kernel(Grid g, int b, int T, int S, Pts3 sp,
                                                              Pts3 so, int has_origin, float bw,
-                                                             float bo,
+                                                             float bo, FastBin fb,
                                                              const float* __restrict__ vol,
                                                              float* __restrict__ tr) {
   extern __shared__ float hist[];  // [T][kTS]
@@ -104,8 +234,7 @@ __global__ void __launch_bounds__(256) velten_adjoint_kernel(Grid g, int b, int 
       const float val = __ldg(vb + v);
       if (val == 0.f) continue;
       const int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((int64_t)g.W * g.H));
-      const float sv = xlen(xsub3(q, voxel_point(g, x, y, z)));
-      const int t = nearest_bin(xadd(od2, xmul(2.f, sv)), bw, bo);
+      const int t = velten_bin(q, od2, voxel_point(g, x, y, z), bw, bo, fb);
       if (t >= 0 && t < T) atomicAdd(hist + t * kTS + sl, val);
     }
   }
@@ -283,12 +412,23 @@ int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
   const int T = (int)transient->shape[1];
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   if (nv == 0 || B == 0) return TOTRI_OK;
-  for (int b = 0; b < (int)B; ++b)
-    TOTRI_KERNEL("backprojection velten confocal", stream,
-                 bp::velten_confocal_kernel<<<(unsigned)ceil_div(nv, 256), 256, 0, stream>>>(
-                     g, b, T, (int)S, sp, so, So > 0, bw, bo,
-                     static_cast<const float*>(transient->data),
-                     static_cast<float*>(volume->data)));
+  const dim3 grid((unsigned)ceil_div(g.W, bp::kBX), (unsigned)ceil_div(g.H, bp::kBY),
+                  (unsigned)ceil_div(g.D, bp::kBZ));
+  const bool tiled = tune::get("backprojection.velten.mode") != 1;
+  for (int b = 0; b < (int)B; ++b) {
+    if (tiled)
+      TOTRI_KERNEL("backprojection velten confocal", stream,
+                   bp::velten_confocal_tiled_kernel<<<grid, 256, 0, stream>>>(
+                       g, b, T, (int)S, sp, so, So > 0, bw, bo, bp::make_fast_bin(bw, bo),
+                       static_cast<const float*>(transient->data),
+                       static_cast<float*>(volume->data)));
+    else
+      TOTRI_KERNEL("backprojection velten confocal", stream,
+                   bp::velten_confocal_kernel<<<(unsigned)ceil_div(nv, 256), 256, 0, stream>>>(
+                       g, b, T, (int)S, sp, so, So > 0, bw, bo, bp::make_fast_bin(bw, bo),
+                       static_cast<const float*>(transient->data),
+                       static_cast<float*>(volume->data)));
+  }
   return TOTRI_OK;
 }
 
@@ -323,7 +463,7 @@ int totri_backprojection_confocal_velten_adjoint(const totri_array_t* volume,
   for (int b = 0; b < (int)B; ++b)
     TOTRI_KERNEL("backprojection velten adjoint", stream,
                  bp::velten_adjoint_kernel<<<(unsigned)ceil_div(S, bp::kTS), 256, smem, stream>>>(
-                     g, b, T, (int)S, sp, so, So > 0, bw, bo,
+                     g, b, T, (int)S, sp, so, So > 0, bw, bo, bp::make_fast_bin(bw, bo),
                      static_cast<const float*>(volume->data),
                      static_cast<float*>(transient->data)));
   return TOTRI_OK;

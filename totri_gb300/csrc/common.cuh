@@ -79,6 +79,19 @@ struct View3i {  // [B, N, 3] int32 or int64
 // index) is built from these so that the CPU oracle (compiled with
 // -ffp-contract=off, fma only where written) reproduces it bit for bit.
 
+// Three-input minimum / maximum (PTX min.f32 / max.f32 with three sources,
+// sm_100 and later): one instruction where two nested fminf/fmaxf take two.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 __device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }

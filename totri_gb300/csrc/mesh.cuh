@@ -53,6 +53,7 @@ struct Scene {
   int* iparent;    // [B][F]
   int* counter;    // [B][F]
   uint32_t* mask;  // [B][P][nch]
+  uint32_t* pscratch;  // [4][B][P]: wall-point sort keys/values (ping-pong)
   uint32_t* status;
   int sorted_buf;  // which ping-pong half holds the sorted keys (0/1)
 };
@@ -69,7 +70,8 @@ struct BuildInputs {
 
 // Workspace layout on the host.
 struct Layout {
-  size_t header, meta, keys, vals, tri, shade, nodes, lparent, iparent, counter, mask, total;
+  size_t header, meta, keys, vals, tri, shade, nodes, lparent, iparent, counter, mask, pscratch,
+      total;
 };
 
 inline Layout layout(int64_t B, int64_t F, int64_t P) {
@@ -93,6 +95,7 @@ inline Layout layout(int64_t B, int64_t F, int64_t P) {
   L.iparent = take(sizeof(int) * B * Fc);
   L.counter = take(sizeof(int) * B * Fc);
   L.mask = take(sizeof(uint32_t) * B * P * nch);
+  L.pscratch = take(sizeof(uint32_t) * 4 * B * P);
   L.total = off;
   return L;
 }
@@ -116,6 +119,7 @@ inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
   s.iparent = reinterpret_cast<int*>(base + L.iparent);
   s.counter = reinterpret_cast<int*>(base + L.counter);
   s.mask = reinterpret_cast<uint32_t*>(base + L.mask);
+  s.pscratch = reinterpret_cast<uint32_t*>(base + L.pscratch);
   s.sorted_buf = 1;  // three 10-bit radix passes end in the second half
   return s;
 }
@@ -123,16 +127,22 @@ inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
 // A scene whose BVH and face records live in `ws` (laid out for zero wall
 // points) and whose visibility masks [B][P][nch] live in a separate buffer:
 // the resident form, where one BVH serves many wall grids.
+inline size_t mask_words_bytes(int64_t B, int64_t F, int64_t P) {
+  const int64_t Fc = F > 0 ? F : 1;
+  return align_up(sizeof(uint32_t) * (size_t)B * (size_t)P * (size_t)((Fc + 31) / 32), 256);
+}
+
+// Mask buffer of the resident form: the masks, then the wall-point sort scratch.
+inline size_t mask_bytes(int64_t B, int64_t F, int64_t P) {
+  return mask_words_bytes(B, F, P) + sizeof(uint32_t) * 4 * (size_t)B * (size_t)P;
+}
+
 inline Scene scene_with_masks(void* ws, int64_t B, int64_t F, void* masks, int64_t P) {
   Scene s = scene_from_workspace(ws, B, F, 0);
   s.P = (int)P;
   s.mask = static_cast<uint32_t*>(masks);
+  s.pscratch = reinterpret_cast<uint32_t*>(static_cast<char*>(masks) + mask_words_bytes(B, F, P));
   return s;
-}
-
-inline size_t mask_bytes(int64_t B, int64_t F, int64_t P) {
-  const int64_t Fc = F > 0 ? F : 1;
-  return sizeof(uint32_t) * (size_t)B * (size_t)P * (size_t)((Fc + 31) / 32);
 }
 
 // ---------------------------------------------------------------------------
@@ -177,18 +187,20 @@ __device__ __forceinline__ bool tri_hit(float4 t0, float4 t1, float4 t2, float4 
   return true;
 }
 
-// Slab test of a BVH box against the ray segment [0, limit]. Boxes carry a
+// Slab test of a BVH box against the ray segment (-inf, limit]. Boxes carry a
 // margin of at least delta beyond every accepted hit point, which dominates
-// the rounding of this test, so a box holding a hit is never rejected.
+// the rounding of this test, so a box holding a hit is never rejected. The
+// entry distance is not clamped at 0: that only admits boxes lying wholly
+// behind the wall point (none do for a mesh in front of the wall), never
+// rejects one, and saves an instruction per box.
 __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy,
                                      float hz, fv3 inv, fv3 oinv, float limit,
                                      float& tnear) {
   const float tx0 = fmaf(lx, inv.x, -oinv.x), tx1 = fmaf(hx, inv.x, -oinv.x);
   const float ty0 = fmaf(ly, inv.y, -oinv.y), ty1 = fmaf(hy, inv.y, -oinv.y);
   const float tz0 = fmaf(lz, inv.z, -oinv.z), tz1 = fmaf(hz, inv.z, -oinv.z);
-  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
-  const float tf =
-      fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), limit));
+  const float tn = fmax3(fminf(tx0, tx1), fminf(ty0, ty1), fminf(tz0, tz1));
+  const float tf = fmin3(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), limit));
   tnear = tn;
   return tn <= tf;
 }

@@ -149,18 +149,15 @@ __global__ void morton_kernel(Scene sc, BuildInputs in) {
 // Stable LSD radix sort of n (key, value) pairs, 3 passes of 10 bits, one CTA
 // of 1024 threads per mesh. Ranks within a tile of 1024 keys come from
 // warp-level digit matching plus a per-digit scan across the 32 warps.
-__global__ void __launch_bounds__(kSortThreads) sort_kernel(Scene sc) {
-  extern __shared__ uint32_t smem[];
+// One-CTA LSD radix sort of n 30-bit keys with their values: three 10-bit
+// passes k0/v0 -> k1/v1 -> k0/v0 -> k1/v1, so the sorted pairs end in k1/v1.
+// Stable; ranks within a warp come from __match_any_sync.
+__device__ void cta_radix_sort30(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int n,
+                                 uint32_t* smem) {
   uint32_t* wcount = smem;                        // [32][1024]
   uint32_t* offset = smem + 32 * kSortDigits;     // [1024] running digit offset
   uint32_t* total = offset + kSortDigits;         // [1024] digit count in tile
-  const int b = blockIdx.x;
-  const int n = sc.meta[b].n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  uint32_t* k0 = sc.keys + (size_t)b * 2 * sc.F;
-  uint32_t* v0 = sc.vals + (size_t)b * 2 * sc.F;
-  uint32_t* k1 = k0 + sc.F;
-  uint32_t* v1 = v0 + sc.F;
   for (int i = tid; i < 32 * kSortDigits; i += kSortThreads) wcount[i] = 0;
   for (int pass = 0; pass < 3; ++pass) {
     const int shift = pass * kSortBits;
@@ -230,6 +227,60 @@ __global__ void __launch_bounds__(kSortThreads) sort_kernel(Scene sc) {
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(kSortThreads) sort_kernel(Scene sc) {
+  extern __shared__ uint32_t smem[];
+  const int b = blockIdx.x;
+  uint32_t* k0 = sc.keys + (size_t)b * 2 * sc.F;
+  uint32_t* v0 = sc.vals + (size_t)b * 2 * sc.F;
+  cta_radix_sort30(k0, v0, k0 + sc.F, v0 + sc.F, sc.meta[b].n, smem);
+}
+
+// Morton order of P wall points, one CTA per batch item: bounding box, 30-bit
+// codes over it, radix sort. scr is [4][B][P] (keys, values, keys, values);
+// the permutation (point indices in Morton order) ends in the fourth quarter.
+__global__ void __launch_bounds__(kSortThreads) point_order_kernel(View3f pts, int P, int B,
+                                                                  uint32_t* scr) {
+  extern __shared__ uint32_t smem[];
+  __shared__ int box[6];
+  const int b = blockIdx.x;
+  const size_t BP = (size_t)B * P;
+  uint32_t* k0 = scr + (size_t)b * P;
+  uint32_t* v0 = scr + BP + (size_t)b * P;
+  uint32_t* k1 = scr + 2 * BP + (size_t)b * P;
+  uint32_t* v1 = scr + 3 * BP + (size_t)b * P;
+  if (threadIdx.x < 3) {
+    box[threadIdx.x] = ford(3.0e38f);
+    box[3 + threadIdx.x] = ford(-3.0e38f);
+  }
+  __syncthreads();
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  for (int i = threadIdx.x; i < P; i += blockDim.x)
+    for (int a = 0; a < 3; ++a) {
+      const float c = pts.at(b, i, a);
+      lo[a] = fminf(lo[a], c);
+      hi[a] = fmaxf(hi[a], c);
+    }
+  for (int a = 0; a < 3; ++a) {
+    atomicMin(&box[a], ford(lo[a]));
+    atomicMax(&box[3 + a], ford(hi[a]));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+      const float l = iord(box[a]), ext = iord(box[3 + a]) - l;
+      float u = ext > 0.f ? (pts.at(b, i, a) - l) / ext : 0.f;
+      u = fminf(fmaxf(u, 0.f), 1.f);
+      if (!(u == u)) u = 0.f;
+      q[a] = (uint32_t)fminf(u * 1024.f, 1023.f);
+    }
+    k0[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    v0[i] = (uint32_t)i;
+  }
+  __syncthreads();
+  cta_radix_sort30(k0, v0, k1, v1, P, smem);
 }
 
 __global__ void records_kernel(Scene sc, BuildInputs in) {
@@ -343,6 +394,20 @@ __global__ void refit_kernel(Scene sc) {
 }
 
 }  // namespace
+
+int launch_point_order(const Scene& sc, const View3f& pts, int P, cudaStream_t stream) {
+  const size_t smem = sizeof(uint32_t) * (32 * kSortDigits + 2 * kSortDigits);
+  static bool attr_set = false;
+  if (!attr_set) {
+    TOTRI_CUDA(cudaFuncSetAttribute(point_order_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  TOTRI_KERNEL("mesh point order", stream,
+               point_order_kernel<<<sc.B, kSortThreads, smem, stream>>>(pts, P, sc.B,
+                                                                         sc.pscratch));
+  return TOTRI_OK;
+}
 
 int build_scene(const Scene& sc, const BuildInputs& in, cudaStream_t stream) {
   const int B = sc.B;

@@ -27,7 +27,7 @@ namespace {
 
 // One warp per (wall point, 32 Morton-consecutive faces): the 32 rays share
 // their origin and end on a compact patch of the surface, so they walk
-// largely the same BVH nodes. kVisRayPostponed (the default) lets each lane
+// largely the same BVH nodes. kVisRayPostponed lets each lane
 // walk alone with its triangle tests postponed until the warp runs them
 // together (target_visible_pp; 22.8 ms against 27.0 ms for kVisRay, the plain
 // per-lane walk target_visible, on the 20,480-face sphere seen from a 64x64
@@ -38,6 +38,8 @@ constexpr int kVisBrute = 0;
 constexpr int kVisRay = 1;
 constexpr int kVisPacket = 2;
 constexpr int kVisRayPostponed = 3;
+constexpr int kVisPatch = 4;
+constexpr int kVisPatchPacket = 5;
 
 template <int kMode>
 __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
@@ -69,6 +71,48 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
   }
   const uint32_t word = __ballot_sync(0xffffffffu, vis);
   if (lane == 0) sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
+}
+
+// One CTA per (block of 32 wall points in Morton order, 32-face chunk): each
+// warp takes one face of the chunk at a time and its 32 lanes cast the rays
+// from the 32 points, which lie on a compact patch of the wall and end on the
+// same centroid, so the lanes walk nearly the same BVH nodes (lockstep model on
+// the 20,480-face sphere: 12% fewer warp iterations and 8.3 -> 5.7 distinct
+// nodes per iteration against point-major warps; measured 15.5 ms against
+// 22.8 ms for point-major warps with the same postponed-leaf walk). The
+// 32 x 32 bits are transposed in shared memory into one mask word per point.
+// This is the default visibility kernel.
+template <bool kPacket>
+__global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f pts, int P,
+                                                               int row0) {
+  __shared__ uint32_t bits[32];  // face j of the chunk: visible from point lane
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = blockIdx.z;
+  const int ch = blockIdx.y;
+  const int i = blockIdx.x * 32 + lane;  // position in Morton order
+  const int n = sc.meta[b].n;
+  const bool okp = i < P;
+  const uint32_t* order = sc.pscratch + 3 * (size_t)sc.B * P + (size_t)b * P;
+  const int p = okp ? (int)order[i] : 0;
+  const fv3 o = okp ? mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2)) : mkv(0.f, 0.f, 0.f);
+  for (int j = warp; j < 32; j += 8) {
+    const int k = ch * 32 + j;
+    bool vis = false;
+    if (k < n) {  // warp-uniform
+      const Target tg = load_target(sc, b, k);
+      if (kPacket) vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
+      else if (okp) vis = target_visible_pp(sc, b, n, tg, o, sc.status);
+    }
+    const uint32_t w = __ballot_sync(0xffffffffu, vis);
+    if (lane == 0) bits[j] = w;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && okp) {
+    uint32_t word = 0u;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) word |= ((bits[j] >> lane) & 1u) << j;
+    sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
+  }
 }
 
 // Per-pair confocal geometry: FP32 decisions exactly as the oracle takes them.
@@ -276,10 +320,21 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
   } else if (tune::get("mesh.visibility.mode") == kVisPacket) {
     TOTRI_KERNEL("mesh visibility", stream,
                  visibility_kernel<kVisPacket><<<blocks, 256, 0, stream>>>(sc, pts, P, row0));
-  } else {
+  } else if (tune::get("mesh.visibility.mode") == kVisRayPostponed) {
     TOTRI_KERNEL("mesh visibility", stream,
                  visibility_kernel<kVisRayPostponed><<<blocks, 256, 0, stream>>>(sc, pts, P,
                                                                                   row0));
+  } else {
+    if (P >= (1 << 30) / 4) return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points");
+    const int st = launch_point_order(sc, pts, P, stream);
+    if (st != TOTRI_OK) return st;
+    const dim3 grid((unsigned)ceil_div(P, 32), (unsigned)sc.nch, (unsigned)sc.B);
+    if (tune::get("mesh.visibility.mode") == kVisPatchPacket)
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<true><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+    else
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<false><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
   }
   return TOTRI_OK;
 }

@@ -227,6 +227,8 @@ __device__ __forceinline__ void scatter_face_grad(const GradOut& out, int b, flo
 // Host launchers.
 int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool brute,
                       cudaStream_t stream);
+// Morton order of P wall points into sc.pscratch ([4][B][P]; order in the last quarter).
+int launch_point_order(const Scene& sc, const View3f& pts, int P, cudaStream_t stream);
 // Wall-to-origin terms of the exhaustive renderer (detector and laser).
 struct Origins {
   View3f so, lo;
