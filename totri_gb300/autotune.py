@@ -21,8 +21,8 @@ CANDIDATES = {
     # 1 per-lane BVH walk, 2 warp-packet walk, 3 per-lane with postponed leaf tests
     # (point-major warps), 4 postponed leaf tests with face-major warps over
     # Morton-ordered wall-point patches (the built-in choice), 5 the same warps
-    # walking as one packet
-    "mesh.visibility.mode": (3, 4, 5),
+    # walking as one packet, 6 the same warps over the 4-wide tree
+    "mesh.visibility.mode": (3, 4, 6),
     "mesh.confocal.splat.ts": (1, 2, 4, 8, 16),
     "mesh.exhaustive.splat.lt": (1, 4, 8, 16, 32),
 }

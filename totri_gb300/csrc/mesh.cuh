@@ -49,6 +49,7 @@ struct Scene {
   float4* tri;     // [B][F][4]
   float4* shade;   // [B][F][4]
   float4* nodes;   // [B][F][4] (F-1 used)
+  float4* wide;    // [B][F][8]: 4-wide nodes at the even-depth binary nodes
   int* lparent;    // [B][F]
   int* iparent;    // [B][F]
   int* counter;    // [B][F]
@@ -70,8 +71,8 @@ struct BuildInputs {
 
 // Workspace layout on the host.
 struct Layout {
-  size_t header, meta, keys, vals, tri, shade, nodes, lparent, iparent, counter, mask, pscratch,
-      total;
+  size_t header, meta, keys, vals, tri, shade, nodes, wide, lparent, iparent, counter, mask,
+      pscratch, total;
 };
 
 inline Layout layout(int64_t B, int64_t F, int64_t P) {
@@ -91,6 +92,7 @@ inline Layout layout(int64_t B, int64_t F, int64_t P) {
   L.tri = take(64 * B * Fc);
   L.shade = take(64 * B * Fc);
   L.nodes = take(64 * B * Fc);
+  L.wide = take(128 * B * Fc);
   L.lparent = take(sizeof(int) * B * Fc);
   L.iparent = take(sizeof(int) * B * Fc);
   L.counter = take(sizeof(int) * B * Fc);
@@ -115,6 +117,7 @@ inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
   s.tri = reinterpret_cast<float4*>(base + L.tri);
   s.shade = reinterpret_cast<float4*>(base + L.shade);
   s.nodes = reinterpret_cast<float4*>(base + L.nodes);
+  s.wide = reinterpret_cast<float4*>(base + L.wide);
   s.lparent = reinterpret_cast<int*>(base + L.lparent);
   s.iparent = reinterpret_cast<int*>(base + L.iparent);
   s.counter = reinterpret_cast<int*>(base + L.counter);
@@ -363,6 +366,106 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
       } else {
         node = pop();
       }
+      if (node < 0 && node != kDone && leaf == kDone) {
+        leaf = node;
+        node = pop();
+      }
+      if (!__any_sync(__activemask(), leaf == kDone)) break;
+    }
+    while (leaf != kDone) {
+      const int kk = ~leaf;
+      if (kk != k) {
+        if (kk < 0 || kk >= n) {
+          atomicOr(status, kStatusTraversalCap);
+        } else {
+          const float4* q = tri_at(sc, b, kk);
+          const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+          float tq;
+          if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
+              (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
+            return false;
+        }
+      }
+      leaf = kDone;
+      if (node < 0 && node != kDone) {
+        leaf = node;
+        node = pop();
+      }
+    }
+  }
+  return true;
+}
+
+// target_visible_pp over the 4-wide tree: each binary node at even depth
+// holds its (up to) four grandchildren, or a child leaf in place of two, as
+// one 128-byte record (boxes as four lanes of SoA float4s, then the four child
+// codes; an empty slot has an inverted box). A step tests four boxes, goes on
+// with the nearest hit and stacks the others, so a ray takes about half the
+// dependent node fetches of the binary walk. The leaves tested, and the
+// answer, are those of target_visible: a leaf is reached iff its binary
+// ancestors' boxes and its own all pass, and the grandchild boxes are the same
+// boxes the binary walk tests.
+constexpr int kWideEmpty = INT_MIN + 1;
+
+__device__ __forceinline__ bool target_visible_pp4(const Scene& sc, int b, int n,
+                                                   const Target& tg, fv3 o, uint32_t* status) {
+  constexpr int kDone = INT_MIN;
+  const int k = tg.k;
+  const fv3 D = xsub3(tg.c, o);
+  const float dist = xlen(D);
+  if (!(dist >= 1e-6f)) return false;
+  const fv3 dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+  const float tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+  const int f = tg.f;
+  float tf;
+  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return false;
+  if (n == 1) return true;
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const float4* wb = sc.wide + (size_t)b * sc.F * 8;
+  int stack[64];
+  int sp = 0;
+  auto push = [&](int v) {
+    if (sp < 64) stack[sp++] = v;
+    else atomicOr(status, kStatusTraversalCap);
+  };
+  auto pop = [&]() { return sp > 0 ? stack[--sp] : kDone; };
+  int node = 0;
+  int leaf = kDone;
+  const int cap = 2 * n + 64;
+  int it = 0;
+  while (node != kDone) {
+    while (node >= 0) {
+      if (++it > cap || node >= n - 1) {
+        atomicOr(status, kStatusTraversalCap);
+        return true;
+      }
+      const float4* w = wb + (size_t)node * 8;
+      const float4 lx = __ldg(w), ly = __ldg(w + 1), lz = __ldg(w + 2);
+      const float4 hx = __ldg(w + 3), hy = __ldg(w + 4), hz = __ldg(w + 5);
+      const float4 cc = __ldg(w + 6);
+      const int c0 = __float_as_int(cc.x), c1 = __float_as_int(cc.y);
+      const int c2 = __float_as_int(cc.z), c3 = __float_as_int(cc.w);
+      float t0, t1, t2, t3;
+      const bool h0 = slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, inv, oinv, tf, t0);
+      const bool h1 = slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, inv, oinv, tf, t1) &&
+                      c1 != kWideEmpty;
+      const bool h2 = slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, inv, oinv, tf, t2) &&
+                      c2 != kWideEmpty;
+      const bool h3 = slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, inv, oinv, tf, t3) &&
+                      c3 != kWideEmpty;
+      // the nearest hit goes on; the other hits are stacked
+      float best = INFINITY;
+      int next = kDone;
+      if (h0 && t0 < best) { best = t0; next = c0; }
+      if (h1 && t1 < best) { best = t1; next = c1; }
+      if (h2 && t2 < best) { best = t2; next = c2; }
+      if (h3 && t3 < best) { best = t3; next = c3; }
+      if (h3 && next != c3) push(c3);
+      if (h2 && next != c2) push(c2);
+      if (h1 && next != c1) push(c1);
+      if (h0 && next != c0) push(c0);
+      node = next != kDone ? next : pop();
       if (node < 0 && node != kDone && leaf == kDone) {
         leaf = node;
         node = pop();

@@ -395,6 +395,45 @@ __global__ void refit_kernel(Scene sc) {
 
 }  // namespace
 
+// 4-wide node records at the even-depth binary nodes: a binary node's child
+// boxes are replaced by its grandchildren's (a leaf child keeps its own box and
+// slot), read after the refit has finished every box. Slots 0 and 1 are always
+// filled; an unused slot carries the code kWideEmpty (traversals skip it).
+__global__ void widen_kernel(Scene sc) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = sc.meta[b].n;
+  if (i >= n - 1) return;
+  const size_t base = (size_t)b * sc.F;
+  int depth = 0;
+  for (int q = sc.iparent[base + i]; q >= 0 && depth < 4096; q = sc.iparent[base + q]) ++depth;
+  if (depth & 1) return;
+  const float* nd = reinterpret_cast<const float*>(sc.nodes + (base + i) * 4);
+  float box[6][4];
+  int code[4] = {kWideEmpty, kWideEmpty, kWideEmpty, kWideEmpty};
+  for (int a = 0; a < 6; ++a)
+    for (int m = 0; m < 4; ++m) box[a][m] = 0.f;
+  int m = 0;
+  for (int side = 0; side < 2; ++side) {
+    const int c = __float_as_int(nd[12 + side]);
+    if (c < 0 || c >= n - 1) {  // leaf (or malformed link: walked and flagged later)
+      for (int a = 0; a < 6; ++a) box[a][m] = nd[6 * side + a];
+      code[m++] = c;
+    } else {
+      const float* cn = reinterpret_cast<const float*>(sc.nodes + (base + c) * 4);
+      for (int g = 0; g < 2; ++g) {
+        for (int a = 0; a < 6; ++a) box[a][m] = cn[6 * g + a];
+        code[m++] = __float_as_int(cn[12 + g]);
+      }
+    }
+  }
+  float4* w = sc.wide + (base + i) * 8;
+  for (int a = 0; a < 6; ++a) w[a] = make_float4(box[a][0], box[a][1], box[a][2], box[a][3]);
+  w[6] = make_float4(__int_as_float(code[0]), __int_as_float(code[1]), __int_as_float(code[2]),
+                     __int_as_float(code[3]));
+  w[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 int launch_point_order(const Scene& sc, const View3f& pts, int P, cudaStream_t stream) {
   const size_t smem = sizeof(uint32_t) * (32 * kSortDigits + 2 * kSortDigits);
   static bool attr_set = false;
@@ -430,6 +469,7 @@ int build_scene(const Scene& sc, const BuildInputs& in, cudaStream_t stream) {
     TOTRI_KERNEL("mesh records", stream, records_kernel<<<gridF, blk, 0, stream>>>(sc, in));
     TOTRI_KERNEL("mesh hierarchy", stream, hierarchy_kernel<<<gridF, blk, 0, stream>>>(sc));
     TOTRI_KERNEL("mesh refit", stream, refit_kernel<<<gridF, blk, 0, stream>>>(sc));
+    TOTRI_KERNEL("mesh widen", stream, widen_kernel<<<gridF, blk, 0, stream>>>(sc));
   }
   return TOTRI_OK;
 }

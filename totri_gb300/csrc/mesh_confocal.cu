@@ -40,6 +40,7 @@ constexpr int kVisPacket = 2;
 constexpr int kVisRayPostponed = 3;
 constexpr int kVisPatch = 4;
 constexpr int kVisPatchPacket = 5;
+constexpr int kVisPatchWide = 6;
 
 template <int kMode>
 __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, int P, int row0) {
@@ -78,11 +79,13 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
 // from the 32 points, which lie on a compact patch of the wall and end on the
 // same centroid, so the lanes walk nearly the same BVH nodes (lockstep model on
 // the 20,480-face sphere: 12% fewer warp iterations and 8.3 -> 5.7 distinct
-// nodes per iteration against point-major warps; measured 15.5 ms against
-// 22.8 ms for point-major warps with the same postponed-leaf walk). The
-// 32 x 32 bits are transposed in shared memory into one mask word per point.
-// This is the default visibility kernel.
-template <bool kPacket>
+// nodes per iteration against point-major warps; measured 15.3 ms against
+// 22.6 ms for point-major warps with the same postponed-leaf walk). The eight
+// warps of a CTA work on neighbouring faces from the same points, so they share
+// their BVH nodes in L1 (a variant without the CTA, one warp per 32 x 32 block,
+// took 23.2 ms). The 32 x 32 bits are transposed in shared memory into one
+// mask word per point. This is the default visibility kernel.
+template <int kWalk>  // 0: target_visible_pp, 1: packet_visible, 2: target_visible_pp4
 __global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f pts, int P,
                                                                int row0) {
   __shared__ uint32_t bits[32];  // face j of the chunk: visible from point lane
@@ -100,8 +103,9 @@ __global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f 
     bool vis = false;
     if (k < n) {  // warp-uniform
       const Target tg = load_target(sc, b, k);
-      if (kPacket) vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
-      else if (okp) vis = target_visible_pp(sc, b, n, tg, o, sc.status);
+      if (kWalk == 1) vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
+      else if (kWalk == 2) vis = okp && target_visible_pp4(sc, b, n, tg, o, sc.status);
+      else vis = okp && target_visible_pp(sc, b, n, tg, o, sc.status);
     }
     const uint32_t w = __ballot_sync(0xffffffffu, vis);
     if (lane == 0) bits[j] = w;
@@ -245,6 +249,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
                                                    const float* __restrict__ tgrad, int T, int S,
                                                    float bw, float bo, GradOut out) {
   extern __shared__ uint32_t mcol[];  // [slice] mask words of this 32-face chunk
+  __shared__ int gq[8][64];           // per-warp queue of visible scan points
   const int b = blockIdx.y;
   const int ch = blockIdx.x;
   const int n = sc.meta[b].n;
@@ -266,8 +271,7 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
     const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
     fv3 acc[3] = {mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f), mkv(0.f, 0.f, 0.f)};
     float accm = 0.f;
-    for (int s = s0 + lane; s < s1; s += 32) {
-      if (!((mcol[s - s0] >> j) & 1u)) continue;
+    auto run = [&](int s) {
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       float od = 0.f;
       if (has_origin)
@@ -276,10 +280,32 @@ __global__ void __launch_bounds__(256) grad_kernel(Scene sc, View3f sp, View3f s
       confocal_pair(s0r, s1r, s2r, p, od, bw, bo, q);
       fv3 dv[3];
       float dm;
-      if (!pair_grad_confocal(q, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) continue;
+      if (!pair_grad_confocal(q, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) return;
       add_permuted(acc, dv, q.perm);
       accm += dm;
+    };
+    // visible scan points are queued and evaluated 32 at a time, one per lane
+    int* qw = gq[warp];
+    int cnt = 0;  // warp-uniform
+    for (int base = s0; base < s1; base += 32) {
+      const int s = base + lane;
+      const bool v = s < s1 && ((mcol[s - s0] >> j) & 1u);
+      const uint32_t bits = __ballot_sync(0xffffffffu, v);
+      if (v) qw[cnt + __popc(bits & ((1u << lane) - 1u))] = s;
+      cnt += __popc(bits);
+      if (cnt >= 32) {
+        __syncwarp();
+        const int e = qw[lane];
+        __syncwarp();
+        if (lane < cnt - 32) qw[lane] = qw[32 + lane];
+        cnt -= 32;
+        __syncwarp();
+        run(e);
+      }
     }
+    __syncwarp();
+    if (lane < cnt) run(qw[lane]);
+    __syncwarp();
     scatter_face_grad(out, b, s1r, s2r, s3r, acc, accm, sc.status);
   }
 }
@@ -329,12 +355,16 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
     const int st = launch_point_order(sc, pts, P, stream);
     if (st != TOTRI_OK) return st;
     const dim3 grid((unsigned)ceil_div(P, 32), (unsigned)sc.nch, (unsigned)sc.B);
-    if (tune::get("mesh.visibility.mode") == kVisPatchPacket)
+    const int mode = tune::get("mesh.visibility.mode");
+    if (mode == kVisPatchPacket)
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<true><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+                   visibility_patch_kernel<1><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+    else if (mode == kVisPatchWide)
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<2><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
     else
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<false><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+                   visibility_patch_kernel<0><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
   }
   return TOTRI_OK;
 }
@@ -393,7 +423,7 @@ int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, in
       tune::grad_split("mesh.confocal.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
   const size_t smem = sizeof(uint32_t) * (size_t)ceil_div(S, split);
   static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
+  if (smem > 40 * 1024 && configured < (int)smem) {  // 2 KB of static shared memory besides
     TOTRI_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
     configured = (int)smem;

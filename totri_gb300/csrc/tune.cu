@@ -38,7 +38,9 @@ int grad_split(const char* key, int64_t ctas, int S, int max_slice) {
   if (most < least) most = least;
   int split = get(key);
   if (split <= 0) {
-    const int64_t target = (int64_t)sm_count() * 8;
+    // gradient CTAs run long (32 faces x a slice of every wall point): aim for
+    // many waves so the last one is short
+    const int64_t target = (int64_t)sm_count() * 32;
     split = ctas > 0 ? (int)((target + ctas - 1) / ctas) : 1;
   }
   if (split > most) split = most;

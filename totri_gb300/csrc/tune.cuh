@@ -11,8 +11,8 @@ namespace totri {
 namespace tune {
 int get(const char* key);  // 0 when unset
 int sm_count();            // multiprocessors of the current device
-// Slices of the scan-point loop for a gradient grid of `ctas` CTAs: enough to
-// give every SM several CTAs, at most one per 64 points (tuned value first),
+// Slices of the scan-point loop for a gradient grid of `ctas` CTAs: enough for
+// 32 CTAs per SM in total, at most one per 64 points (tuned value first),
 // and never fewer than make each slice at most `max_slice` points long.
 int grad_split(const char* key, int64_t ctas, int S, int max_slice);
 }  // namespace tune
