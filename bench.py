@@ -288,6 +288,16 @@ def batched_metrics(device, count=32, steps=2):
     ms_batched = timed(br.step, steps)
     waves = [len(w.members) for w in br.waves]
     tiles = {str(k): v for k, v in br.tiles.items()}
+    from totri_gb300 import _lib
+    # per-kernel times of the same step launched eagerly (graph replays are
+    # not visible to the library's launch profiler)
+    _lib.profile_reset()
+    _lib.profile_enable(True)
+    with torch.cuda.stream(br.stream):
+        br._step_calls()
+    br.stream.synchronize()
+    _lib.profile_enable(False)
+    kernels_batched = {k: {"launches": v[0], "ms": v[2]} for k, v in _lib.profile_read().items()}
     del br
     torch.cuda.empty_cache()
     so = torch.empty((1, 0, 3), device=device)
@@ -303,7 +313,6 @@ def batched_metrics(device, count=32, steps=2):
                                          bd.width, bd.offset, 0)
 
     plain()
-    from totri_gb300 import _lib
     _lib.profile_reset()
     _lib.profile_enable(True)
     ms_plain = timed(plain, 1)
@@ -312,6 +321,7 @@ def batched_metrics(device, count=32, steps=2):
     torch.cuda.empty_cache()
     return {
         "kernels_plain_pass": kernels,
+        "kernels_batched_eager": kernels_batched,
         "value": triples / (ms_batched / 1e3), "unit": "triples/s", "ms": ms_batched,
         "plain_calls": {"value": triples / (ms_plain / 1e3), "ms": ms_plain},
         "speedup_vs_plain": ms_plain / ms_batched,

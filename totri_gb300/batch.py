@@ -19,9 +19,10 @@ Loss heads (``grad``):
     capture (torch ops on the device), which fills ``transient_grad`` for the
     meshes of the wave (indices into the constructor's list).
 
-Tuned tile values are installed process-wide (``totri_tune_set``) and stay in
-force for later calls; the captured graph keeps the values it was captured
-with.
+Tuned tile values are installed (``totri_tune_set``, a process-wide table)
+only while this renderer launches its own kernels and handed back to the
+built-in choices afterwards; captured graphs keep the values they were
+captured with. Renderers on several threads must not launch concurrently.
 """
 import math
 import typing
@@ -121,7 +122,7 @@ class BatchedMeshRenderer:
                     cls = autotune.shape_class(F=self.sizes[w.members[pos]][1], S=S, T=T, L=L)
                     self.tiles[w.index] = {
                         key: autotune.tune(key, lambda: self._forward_calls(w, pos), cls,
-                                           reps=1)[0]
+                                           reps=2)[0]
                         for key in ("mesh.visibility.mode", splat)}
         self.graph_forward = None
         self.graph_step = None
@@ -136,12 +137,19 @@ class BatchedMeshRenderer:
             self.graph_step = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph_step, stream=self.stream):
                 self._step_calls()
+        self._restore_tiles()
 
     # -- device work -------------------------------------------------------
 
     def _install_tiles(self, w):
         for key, value in self.tiles.get(w.index, {}).items():
             autotune.set_tile(key, value)
+
+    def _restore_tiles(self):
+        """Hands the tuned keys back to the built-in choices (other callers of
+        the library are not affected by this renderer's tuning)."""
+        for key in {k for t in self.tiles.values() for k in t}:
+            autotune.set_tile(key, 0)
 
     def _args(self):
         bd = self.bin_def
@@ -195,6 +203,12 @@ class BatchedMeshRenderer:
             self.grad(list(w.members), tr, self.transient_grad[:n])
 
     def _step_calls(self):
+        try:
+            self._wave_calls()
+        finally:
+            self._restore_tiles()
+
+    def _wave_calls(self):
         for w in self.waves:
             self._forward_calls(w)
             self._loss_head(w)
@@ -227,7 +241,10 @@ class BatchedMeshRenderer:
             self.graph_forward.replay()
         else:
             with torch.cuda.stream(self.stream):
-                self._forward_calls(self.waves[0])
+                try:
+                    self._forward_calls(self.waves[0])
+                finally:
+                    self._restore_tiles()
         self.stream.synchronize()
         return self.transient
 

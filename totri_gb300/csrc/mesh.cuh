@@ -340,15 +340,16 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
   auto pop = [&]() { return sp > 0 ? stack[--sp] : kDone; };
   int node = 0;      // internal node (>= 0), leaf (~k < 0) or kDone
   int leaf = kDone;  // parked leaf
-  const int cap = 2 * n + 64;
-  int it = 0;
+  const float4* nodes = sc.nodes + (size_t)b * sc.F * 4;
+  const unsigned inner = (unsigned)(n - 1);
+  int budget = 2 * n + 64;  // iteration cap: a malformed tree ends the walk
   while (node != kDone) {
     while (node >= 0) {
-      if (++it > cap || node >= n - 1) {  // malformed tree
+      if (--budget < 0 || (unsigned)node >= inner) {  // malformed tree
         atomicOr(status, kStatusTraversalCap);
         return true;
       }
-      const float4* nd = node_at(sc, b, node);
+      const float4* nd = nodes + node * 4;
       const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
       float tn0, tn1;
       const bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);

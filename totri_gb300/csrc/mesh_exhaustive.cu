@@ -454,7 +454,12 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
 int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                            const Origins& org, int S, int L, const float* tgrad, int T, float bw,
                            float bo, const GradOut& out, cudaStream_t stream) {
-  constexpr int kMaxSlice = 16384;
+  // At most 512 scan points per CTA: a warp walks one face over its slice and
+  // then the next face over the same slice, re-reading the same transient_grad
+  // rows (slice x L x the chunk's bins), which then stay in L2 (one 20k-face
+  // mesh, 1024 x 256 wall points: 92 ms with 512-point slices, 139 ms with
+  // 2048).
+  constexpr int kMaxSlice = 512;
   const int split =
       tune::grad_split("mesh.exhaustive.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
   const int64_t slice = ceil_div(S, split);
