@@ -178,3 +178,39 @@ def test_differentiable_workload_visibility_and_forward(cuda_lib):
                             torch.empty_like(d["scan_points"][:, :0]), out, bd.width, bd.offset, 0)
     ref = _oracle_forward(n, bvh, bd)
     assert rel_l2(out[0].double().cpu().numpy(), ref) < FWD_TOL
+
+
+def test_filtered_fast_path_keeps_exact_bins(cuda_lib):
+    """The splat takes vertex order and bins from fast lengths only where a
+    proven margin says the exact chain decides the same; with the fast path off
+    (every pair exact) the full-size transient agrees to FP32 rounding. The
+    gradient always runs the exact chain, so it is unchanged."""
+    from totri_gb300 import autotune
+    s = scenes.confocal_differentiable()
+    d = _dev(s)
+    bd = s["bin_def"]
+    empty = torch.empty_like(d["scan_points"][:, :0])
+    tg = torch.randn((1, bd.num, d["scan_points"].shape[1]), device="cuda",
+                     generator=torch.Generator(device="cuda").manual_seed(3))
+    out = []
+    for exact in (0, 1):
+        autotune.set_tile("mesh.confocal.exact", exact)
+        try:
+            tr = torch.empty((1, bd.num, d["scan_points"].shape[1]), device="cuda")
+            R.mesh_confocal_forward(d["verts"], d["faces"], d["colors"], d["scan_points"], empty,
+                                    tr, bd.width, 0.0137, 0)
+            vg, mg = torch.empty_like(d["verts"]), torch.empty_like(d["colors"])
+            R.mesh_confocal_grad_verts(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                                       empty, tg, vg, mg, bd.width, 0.0137, 0)
+            out.append((tr.cpu(), vg.cpu(), mg.cpu()))
+        finally:
+            autotune.set_tile("mesh.confocal.exact", 0)
+    (a, va, ma), (b, vb, mb) = out
+    # values differ by the few ulps of the bin coordinates (a partial bin's
+    # width (b + 1 - c) moves by one ulp of c, ~1e-4 of that bin's share);
+    # a bin or order taken differently would move whole tent pieces
+    assert rel_l2(a.numpy(), b.numpy()) < 1e-5
+    assert float((a - b).abs().max()) <= 2e-4 * float(b.abs().max())
+    # the gradient takes the exact chain either way (atomic order only)
+    assert rel_l2(va.numpy(), vb.numpy()) < 1e-5
+    assert rel_l2(ma.numpy(), mb.numpy()) < 1e-5

@@ -99,3 +99,35 @@ def test_matches_reference_golden(cuda_lib):
                                  .cuda(), vg, mg, bw, bo, 0)
     assert rel_l2(vg[0].cpu().numpy(), g["verts_grad"]) < 1e-3
     assert rel_l2(mg[0].cpu().numpy(), g["colors_grad"]) < 1e-3
+
+
+def test_filtered_fast_path_keeps_exact_bins(cuda_lib):
+    """The exhaustive kernels decide vertex order and bins from fast lengths
+    only where a proven margin says the exact chain decides the same. With the
+    fast path off every triple takes the exact chain: transients and gradients
+    agree to FP32 rounding."""
+    from totri_gb300 import autotune
+    s, sp, lp, bd = case(seed=4, s_res=8, l_res=4, nb=400, bw=0.0123)
+    d = [s[k].cuda() for k in ("verts", "faces", "colors")]
+    so = torch.empty((1, 0, 3), device="cuda")
+    out = []
+    for exact in (0, 1):
+        autotune.set_tile("mesh.exhaustive.exact", exact)
+        try:
+            tr = torch.empty((1, bd.num, sp.shape[1], lp.shape[1]), device="cuda")
+            R.mesh_exhaustive_forward(*d, sp.cuda(), lp.cuda(), so, so, tr, bd.width, 0.031, 0)
+            vg, mg = torch.empty_like(d[0]), torch.empty_like(d[2])
+            R.mesh_exhaustive_grad_verts(*d, sp.cuda(), lp.cuda(), so, so, tr, vg, mg, bd.width,
+                                         0.031, 0)
+            out.append((tr.cpu(), vg.cpu(), mg.cpu()))
+        finally:
+            autotune.set_tile("mesh.exhaustive.exact", 0)
+    (a, va, ma), (b, vb, mb) = out
+    # values differ by the few ulps of the bin coordinates (a partial bin's
+    # width (b + 1 - c) moves by one ulp of c, ~1e-4 of that bin's share);
+    # a bin or order taken differently would move whole tent pieces
+    assert rel_l2(a.numpy(), b.numpy()) < 1e-5
+    assert float((a - b).abs().max()) <= 2e-4 * float(b.abs().max())
+    # gradients: FP32 cancellation amplifies the few-ulp value differences
+    assert rel_l2(va.numpy(), vb.numpy()) < 1e-4
+    assert rel_l2(ma.numpy(), mb.numpy()) < 1e-4

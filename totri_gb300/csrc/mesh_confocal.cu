@@ -145,6 +145,43 @@ __device__ __forceinline__ void confocal_pair(const float4 s0, const float4 s1, 
   }
 }
 
+// confocal_pair with a filtered fast path (FastBins): lengths from the
+// hardware reciprocal square root, bin coordinates from one fused
+// multiply-add. Each fast length is within 8 u d of the exact chain's
+// (u = 2^-24), so three lengths separated by more than 16 u max(d) sort as the
+// exact ones do, and a bin coordinate farther than
+// 32 u (2d + od + |bo|)/bw + 8 u |c| + 1e-6 from an integer truncates to the
+// exact bin. Only then are the fast values kept; otherwise (ties, NaN, huge
+// coordinates) the exact confocal_pair runs. Bins and vertex order are always
+// those of the exact chain; values differ from it by a few ulps. Used by the
+// forward splat only: the gradient's FP32 cancellation amplifies those ulps
+// (2.8e-4 rel-L2 on the 20,480-face vertex gradient), so the gradient keeps
+// the exact chain.
+__device__ __forceinline__ void confocal_pair_filtered(const float4 s0, const float4 s1,
+                                                       const float4 s2, fv3 sp, float od,
+                                                       float bw, float bo, const FastBins& fb,
+                                                       ConfocalPair& q) {
+  q.v[0] = mkv(s0.x, s0.y, s0.z);
+  q.v[1] = mkv(s1.x, s1.y, s1.z);
+  q.v[2] = mkv(s2.x, s2.y, s2.z);
+  for (int k = 0; k < 3; ++k) {
+    q.perm[k] = k;
+    q.d[k] = len_fast(q.v[k] - sp);
+  }
+  sort3(q);
+  const float u = 5.9604645e-8f;
+  bool ok = q.d[1] - q.d[0] > 16.f * u * q.d[2] && q.d[2] - q.d[1] > 16.f * u * q.d[2];
+  for (int k = 0; k < 3; ++k) {
+    const float x = fmaf(2.f, q.d[k], od);
+    const float c = fmaf(x, fb.inv_bw, fb.nbo);
+    const float m = fmaf(fb.kc, x, fb.kb) + 8.f * u * fabsf(c);
+    ok = ok && fabsf(c - rintf(c)) > m && fabsf(c) < 1.0e9f;
+    q.c[k] = c;
+    q.bin[k] = __float2int_rz(c);
+  }
+  if (!ok) confocal_pair(s0, s1, s2, sp, od, bw, bo, q);
+}
+
 // alpha of AlphaConfocal (mesh_common.h:394-413):
 // 100 rho (n_w.r)^2 (n.r)^2 / (|n| |r|^8), n_w = (0,0,1), r = c - s.
 __device__ __forceinline__ float alpha_confocal(const ConfocalPair& q, fv3 c, fv3 sp,
@@ -160,7 +197,7 @@ __device__ __forceinline__ float alpha_confocal(const ConfocalPair& q, fv3 c, fv
 template <int TS>
 __global__ void __launch_bounds__(256) splat_kernel(Scene sc, View3f sp, View3f so, int has_origin,
                                                     float* __restrict__ transient, int T, int S,
-                                                    float bw, float bo) {
+                                                    float bw, float bo, FastBins fb) {
   extern __shared__ float hist[];  // [T][TS]
   const int b = blockIdx.y;
   const int s0 = blockIdx.x * TS;
@@ -181,7 +218,7 @@ __global__ void __launch_bounds__(256) splat_kernel(Scene sc, View3f sp, View3f 
       const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
       const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
       ConfocalPair q;
-      confocal_pair(s0r, s1r, s2r, p, od, bw, bo, q);
+      confocal_pair_filtered(s0r, s1r, s2r, p, od, bw, bo, fb, q);
       const float alpha = alpha_confocal(q, mkv(s3r.x, s3r.y, s3r.z), p, s0r.w);
       if (!(alpha > 0.f)) continue;
       splat_tent(h, q.c, q.bin, alpha);
@@ -382,8 +419,9 @@ static int launch_splat_ts(const Scene& sc, const View3f& sp, const View3f& so, 
   }
   const dim3 grid((unsigned)ceil_div(S, TS), (unsigned)sc.B);
   TOTRI_KERNEL("mesh confocal splat", stream,
-               splat_kernel<TS><<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, transient, T,
-                                                             S, bw, bo));
+               splat_kernel<TS><<<grid, 256, smem, stream>>>(
+                   sc, sp, so, has_origin, transient, T, S, bw, bo,
+                   make_fast_bins(bw, bo, tune::get("mesh.confocal.exact") != 1)));
   return TOTRI_OK;
 }
 
@@ -404,11 +442,14 @@ int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, i
       default: return fail(TOTRI_ERR_INVALID_ARGUMENT, "scan tile must be 1, 2, 4, 8 or 16");
     }
   }
-  if ((size_t)T * 8 * 4 <= budget && S >= 8 * 152)
+  // Built-in choice: the widest scan tile that keeps the histogram within
+  // 40 KB (several CTAs per SM) and still gives every SM tiles to work on.
+  const size_t kTileBytes = 40 * 1024;
+  if ((size_t)T * 8 * 4 <= kTileBytes && S >= 8 * 152)
     return launch_splat_ts<8>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
-  if ((size_t)T * 4 * 4 <= budget && S >= 4 * 152)
+  if ((size_t)T * 4 * 4 <= kTileBytes && S >= 4 * 152)
     return launch_splat_ts<4>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
-  if ((size_t)T * 2 * 4 <= budget && S >= 2 * 152)
+  if ((size_t)T * 2 * 4 <= kTileBytes && S >= 2 * 152)
     return launch_splat_ts<2>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);
   if ((size_t)T * 4 <= budget)
     return launch_splat_ts<1>(sc, sp, so, has_origin, transient, T, S, bw, bo, stream);

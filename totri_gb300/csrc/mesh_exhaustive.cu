@@ -61,6 +61,42 @@ __device__ __forceinline__ void exh_pair(float4 s0, float4 s1, float4 s2, fv3 sp
   }
 }
 
+// exh_pair with a filtered fast path (FastBins). The six lengths come from
+// the hardware reciprocal square root and the bin coordinates from a fused
+// multiply-add with a precomputed 1/bw. Against the exact chain each path
+// length d = |v - s| + |v - l| deviates by at most 8 u d (u = 2^-24), so when
+// the three fast lengths are separated by more than 16 u max(d) the exact
+// sort gives the same order, and a bin coordinate farther than
+// 32 u (d + od + |bo|)/bw + 8 u |c| from an integer truncates to the exact
+// bin. Only then are the fast values kept (they differ from the exact ones
+// by a few ulps, which the value tolerances absorb); otherwise, and for
+// NaN or huge coordinates, the exact exh_pair runs. Bins and vertex order
+// are therefore always those of the exact chain.
+__device__ __forceinline__ void exh_pair_filtered(float4 s0, float4 s1, float4 s2, fv3 sp,
+                                                  fv3 lp, float od, float bw, float bo,
+                                                  const FastBins& fb, ExhPair& q) {
+  q.v[0] = mkv(s0.x, s0.y, s0.z);
+  q.v[1] = mkv(s1.x, s1.y, s1.z);
+  q.v[2] = mkv(s2.x, s2.y, s2.z);
+  for (int k = 0; k < 3; ++k) {
+    q.perm[k] = k;
+    q.ds[k] = len_fast(q.v[k] - sp);
+    q.dl[k] = len_fast(q.v[k] - lp);
+    q.d[k] = q.ds[k] + q.dl[k];
+  }
+  exh_sort(q);
+  const float u = 5.9604645e-8f;
+  bool ok = q.d[1] - q.d[0] > 16.f * u * q.d[2] && q.d[2] - q.d[1] > 16.f * u * q.d[2];
+  for (int k = 0; k < 3; ++k) {
+    const float c = fmaf(q.d[k] + od, fb.inv_bw, fb.nbo);
+    const float m = fmaf(fb.kc, q.d[k] + od, fb.kb) + 8.f * u * fabsf(c);
+    ok = ok && fabsf(c - rintf(c)) > m && fabsf(c) < 1.0e9f;
+    q.c[k] = c;
+    q.bin[k] = __float2int_rz(c);
+  }
+  if (!ok) exh_pair(s0, s1, s2, sp, lp, od, bw, bo, q);
+}
+
 // AlphaExhaustive (mesh_common.h:505-531), wall normals (0,0,1).
 __device__ __forceinline__ float alpha_exhaustive(const ExhPair& q, fv3 c, fv3 sp, fv3 lp,
                                                   float rho) {
@@ -84,7 +120,7 @@ __device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int
 template <int LT>
 __global__ void __launch_bounds__(256) exh_splat_kernel(Scene sc, View3f sp, View3f lp, Origins org,
                                                         int S, int L, float* __restrict__ out,
-                                                        int T, float bw, float bo) {
+                                                        int T, float bw, float bo, FastBins fb) {
   extern __shared__ float hist[];  // [T][LT]
   const int b = blockIdx.z;
   const int s = blockIdx.x;
@@ -108,7 +144,7 @@ __global__ void __launch_bounds__(256) exh_splat_kernel(Scene sc, View3f sp, Vie
       const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
       const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
       ExhPair e;
-      exh_pair(s0r, s1r, s2r, p, q, od, bw, bo, e);
+      exh_pair_filtered(s0r, s1r, s2r, p, q, od, bw, bo, fb, e);
       const float alpha = alpha_exhaustive(e, mkv(s3r.x, s3r.y, s3r.z), p, q, s0r.w);
       if (!(alpha > 0.f)) continue;
       splat_tent(h, e.c, e.bin, alpha);
@@ -135,7 +171,7 @@ template <int LT>
 __global__ void __launch_bounds__(256) exh_splat_compact_kernel(Scene sc, View3f sp, View3f lp,
                                                                 Origins org, int S, int L,
                                                                 float* __restrict__ out, int T,
-                                                                float bw, float bo) {
+                                                                float bw, float bo, FastBins fb) {
   extern __shared__ float hist[];  // [T][LT]
   __shared__ float lpt[LT][4];     // laser point, laser-origin term
   __shared__ int queue[8][kExhQueue];
@@ -169,7 +205,7 @@ __global__ void __launch_bounds__(256) exh_splat_compact_kernel(Scene sc, View3f
     const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
     const fv3 q = mkv(lpt[l][0], lpt[l][1], lpt[l][2]);
     ExhPair ep;
-    exh_pair(s0r, s1r, s2r, p, q, lpt[l][3], bw, bo, ep);
+    exh_pair_filtered(s0r, s1r, s2r, p, q, lpt[l][3], bw, bo, fb, ep);
     const float alpha = alpha_exhaustive(ep, mkv(s3r.x, s3r.y, s3r.z), p, q, s0r.w);
     if (!(alpha > 0.f)) return;
     const Hist<LT> h{hist, l, T};
@@ -257,7 +293,7 @@ __device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3
 __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View3f lp, Origins org,
                                                        int S, int L,
                                                        const float* __restrict__ tgrad, int T,
-                                                       float bw, float bo, GradOut out) {
+                                                       float bw, float bo, FastBins fb, GradOut out) {
   extern __shared__ uint32_t mcol[];  // [S + L] mask words of this 32-face chunk
   const int b = blockIdx.y;
   const int ch = blockIdx.x;
@@ -288,7 +324,8 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
         if (!((mcol[S + l] >> j) & 1u)) continue;
         const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
         ExhPair e;
-        exh_pair(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, e);
+        exh_pair_filtered(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, fb,
+                          e);
         fv3 dv[3];
         float dm;
         if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
@@ -309,7 +346,7 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
 // gradient stays in registers and is reduced and scattered once per CTA.
 __global__ void __launch_bounds__(256) exh_grad_compact_kernel(
     Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
-    int T, float bw, float bo, GradOut out) {
+    int T, float bw, float bo, FastBins fb, GradOut out) {
   extern __shared__ uint32_t words[];  // [slice] scan words | [32][LW] laser sets
   __shared__ int qs[8][kExhQueue], ql[8][kExhQueue];
   const int b = blockIdx.y;
@@ -350,7 +387,8 @@ __global__ void __launch_bounds__(256) exh_grad_compact_kernel(
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       const fv3 q = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
       ExhPair e;
-      exh_pair(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, e);
+      exh_pair_filtered(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, fb,
+                          e);
       fv3 dv[3];
       float dm;
       if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
@@ -410,7 +448,7 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
     }
     TOTRI_KERNEL("mesh exhaustive splat", stream,
                  exh_splat_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, out, T,
-                                                                   bw, bo));
+                                                                   bw, bo, make_fast_bins(bw, bo, tune::get("mesh.exhaustive.exact") != 1)));
     return TOTRI_OK;
   }
   static int configured = 0;
@@ -420,8 +458,8 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
     configured = (int)smem;
   }
   TOTRI_KERNEL("mesh exhaustive splat", stream,
-               exh_splat_compact_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L,
-                                                                         out, T, bw, bo));
+               exh_splat_compact_kernel<LT><<<grid, 256, smem, stream>>>(
+                   sc, sp, lp, org, S, L, out, T, bw, bo, make_fast_bins(bw, bo, tune::get("mesh.exhaustive.exact") != 1)));
   return TOTRI_OK;
 }
 
@@ -442,8 +480,15 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
       default: return fail(TOTRI_ERR_INVALID_ARGUMENT, "laser tile must be 1, 4, 8, 16 or 32");
     }
   }
-  if ((size_t)T * 16 * 4 <= budget && L >= 16)
+  // Built-in choice: the widest laser tile whose histogram stays within 40 KB,
+  // so several CTAs share an SM (2048 bins x 64x64 x 16x16, 32 meshes: 4.4 s
+  // with 4 lasers per tile, 12.7 s with 16, whose 128 KB tile leaves one CTA
+  // per SM).
+  const size_t kTileBytes = 40 * 1024;
+  if ((size_t)T * 16 * 4 <= kTileBytes && L >= 16)
     return launch_exh_splat<16>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
+  if ((size_t)T * 8 * 4 <= kTileBytes && L >= 8)
+    return launch_exh_splat<8>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
   if ((size_t)T * 4 * 4 <= budget && L >= 4)
     return launch_exh_splat<4>(sc, sp, lp, org, S, L, out, T, bw, bo, stream);
   if ((size_t)T * 4 <= budget)
@@ -478,7 +523,7 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
     const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
     TOTRI_KERNEL("mesh exhaustive grad", stream,
                  exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T,
-                                                              bw, bo, out));
+                                                              bw, bo, make_fast_bins(bw, bo, tune::get("mesh.exhaustive.exact") != 1), out));
     return TOTRI_OK;
   }
   const size_t smem = sizeof(uint32_t) * (size_t)(slice + 32 * ceil_div(L, 32));
@@ -491,8 +536,8 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   }
   const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh exhaustive grad", stream,
-               exh_grad_compact_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad,
-                                                                    T, bw, bo, out));
+               exh_grad_compact_kernel<<<grid, 256, smem, stream>>>(
+                   sc, sp, lp, org, S, L, tgrad, T, bw, bo, make_fast_bins(bw, bo, tune::get("mesh.exhaustive.exact") != 1), out));
   return TOTRI_OK;
 }
 

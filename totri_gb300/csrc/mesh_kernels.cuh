@@ -3,6 +3,8 @@
 // the tent gradient and the per-face gradient scatter.
 #pragma once
 
+#include <cmath>
+
 #include "mesh.cuh"
 
 namespace totri {
@@ -190,6 +192,33 @@ __device__ __forceinline__ float warp_sum(float x) {
 // Reduces one face's gradient over the warp and adds it to its vertices
 // (mesh_confocal_grad_verts_optix.cu:316-332; 1/3 of the albedo gradient
 // goes to channel 0 of each vertex).
+// Constants of the filtered fast paths of the pair/triple geometry: 1/bw,
+// -bo/bw and the two terms of the bin-coordinate margin (32 u / bw and
+// 32 u |bo| / bw + 1e-6, u = 2^-24). A disabled set has infinite margins, so
+// every pair takes the exact chain. The tuning keys "mesh.exhaustive.exact"
+// and "mesh.confocal.exact" = 1 disable them, for comparison.
+struct FastBins {
+  float inv_bw, nbo, kc, kb;
+};
+
+inline FastBins make_fast_bins(float bw, float bo, bool enabled) {
+  const float u = 5.9604645e-8f;
+  FastBins f;
+  f.inv_bw = 1.f / bw;
+  f.nbo = -bo * f.inv_bw;
+  const bool ok = enabled && bw > 0.f && std::isfinite(f.inv_bw) && std::isfinite(f.nbo);
+  f.kc = ok ? 32.f * u * f.inv_bw : INFINITY;
+  f.kb = ok ? 32.f * u * std::fabs(bo) * f.inv_bw + 1e-6f : INFINITY;
+  return f;
+}
+
+// |a| from the hardware reciprocal square root: within 6.5 u of the exact
+// IEEE chain's value (2 ulp rsqrt, one rounding each for the sum and product).
+__device__ __forceinline__ float len_fast(fv3 a) {
+  const float d2 = fmaf(a.x, a.x, fmaf(a.y, a.y, a.z * a.z));
+  return d2 * rsqrtf(d2);
+}
+
 // acc[perm[k]] += dv[k] for a permutation perm of {0, 1, 2}, with selects
 // instead of a dynamically indexed array (which would live in local memory).
 __device__ __forceinline__ void add_permuted(fv3 acc[3], const fv3 dv[3], const int perm[3]) {
