@@ -206,16 +206,18 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
 }
 
 // Exact adjoint of the forward: one CTA per voxel column, threads over
-// points, each walking the bins whose samples land in the column; shared
-// column accumulator.
+// points, each walking the bins whose samples land in the column. Each warp
+// accumulates into its own copy of the column in shared memory (eight copies:
+// the 256 threads' atomics no longer pile onto one Z-vector), summed at the end.
 __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp, int N,
                                                                const float* __restrict__ tr,
                                                                float* __restrict__ vol) {
-  extern __shared__ float col[];  // [Z]
+  extern __shared__ float cols[];  // [8][Z]
   const int c = blockIdx.x;
   const int xi = c / g.Y, yi = c - xi * g.Y;
-  for (int z = threadIdx.x; z < g.Z; z += blockDim.x) col[z] = 0.f;
+  for (int z = threadIdx.x; z < 8 * g.Z; z += blockDim.x) cols[z] = 0.f;
   __syncthreads();
+  float* col = cols + (threadIdx.x >> 5) * g.Z;
   const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
@@ -234,7 +236,11 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
     }
   }
   __syncthreads();
-  for (int z = threadIdx.x; z < g.Z; z += blockDim.x) vol[(size_t)c * g.Z + z] = col[z];
+  for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
+    float sum = 0.f;
+    for (int w = 0; w < 8; ++w) sum += cols[w * g.Z + z];
+    vol[(size_t)c * g.Z + z] = sum;
+  }
 }
 
 // The reference's transposed operator, per voxel (volume_cuda.cu:96-160).
@@ -394,9 +400,16 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
     return TOTRI_OK;
   }
   const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
+  const size_t smem = sizeof(float) * 8 * (size_t)Z;
+  if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "volume too deep for one column tile");
+  static int configured = 0;
+  if (smem > 48 * 1024 && configured < (int)smem) {
+    TOTRI_CUDA(cudaFuncSetAttribute(volume::confocal_adjoint_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = (int)smem;
+  }
   TOTRI_KERNEL("volume confocal adjoint", stream,
-               volume::confocal_adjoint_kernel<<<(unsigned)(X * Y), 256, sizeof(float) * Z,
-                                                 stream>>>(
+               volume::confocal_adjoint_kernel<<<(unsigned)(X * Y), 256, smem, stream>>>(
                    g, pts, N, static_cast<const float*>(tr->data), static_cast<float*>(vol->data)));
   return TOTRI_OK;
 }
