@@ -45,6 +45,11 @@ def flop_visibility(num_faces):
     return 40.0 * math.ceil(math.log2(max(num_faces, 2))) + 144.0
 
 
+# The secondary, batched and serving measurements are single-GPU figures: they
+# run on one-process runs only, so a multi-rank run holds its GPUs just for the
+# headline step.
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -626,13 +631,13 @@ def main():
     e2e_value = world * pairs * e2e_steps / e2e_s
 
     secondary = None
-    if rank == 0 and not args.no_secondary:
+    if rank == 0 and world == 1 and not args.no_secondary:
         secondary = secondary_metrics(device, flush)
     batched = None
-    if rank == 0 and not args.no_batched:
+    if rank == 0 and world == 1 and not args.no_batched:
         batched = batched_metrics(device)
     served = None
-    if rank == 0 and not args.no_serve:
+    if rank == 0 and world == 1 and not args.no_serve:
         served = serve_metrics(device)
 
     cpu = None
