@@ -29,11 +29,17 @@ __device__ __forceinline__ float coord(float s, float e, int n, int i) {
   return n == 1 ? 0.5f * (s + e) : s + ((e - s) * (float)i) / (float)(n - 1);
 }
 
-__device__ __forceinline__ float gaussian(float x, float y, float z, float xr, float yr, float zr,
-                                          float sigma) {
-  const float d2 = (xr - x) * (xr - x) + (yr - y) * (yr - y) + (zr - z) * (zr - z);
-  return expf(-0.5f * d2 / (sigma * sigma));
+// 2^x from the hardware approximation (ex2.approx, relative error about
+// 2^-22; results below the normal range flush to zero): the Gaussians are
+// values, compared with tolerances, and -d2 / (2 sigma^2) folds into one
+// multiply by a per-Gaussian constant -log2(e) / (2 sigma^2).
+__device__ __forceinline__ float exp2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
+
+constexpr float kLog2e = 1.4426950408889634f;
 
 struct Rbf {  // [B, N, C] with strides
   const float* p;
@@ -58,12 +64,17 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
     __syncthreads();
     for (int j = threadIdx.x; j < kTile * C; j += blockDim.x) {
       const int i = j / C, c = j - i * C;
-      if (i0 + i < N) tile[i][c] = r.at(b, i0 + i, c);
+      if (i0 + i < N) {
+        const float val = r.at(b, i0 + i, c);
+        // slot 3 holds -log2(e) / (2 sigma^2) instead of sigma
+        tile[i][c] = c == 3 ? -0.5f * kLog2e / (val * val) : val;
+      }
     }
     __syncthreads();
     const int cnt = min(kTile, N - i0);
     for (int i = 0; i < cnt; ++i) {
-      const float w = gaussian(x, y, z, tile[i][0], tile[i][1], tile[i][2], tile[i][3]);
+      const float dx = tile[i][0] - x, dy = tile[i][1] - y, dz = tile[i][2] - z;
+      const float w = exp2_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * tile[i][3]);
       sum += w;
 #pragma unroll
       for (int a = 0; a < kMaxAttr; ++a)
@@ -108,6 +119,8 @@ __global__ void __launch_bounds__(128) grad_kernel(Grid g, int b, Rbf r, int N, 
       if (a < A) ra[a] = r.at(b, i, 4 + a);
   }
   const float is2 = 1.f / (sigma * sigma);
+  const float k2 = -0.5f * kLog2e * is2;  // w = 2^(d2 * k2)
+  const float is3 = is2 / sigma;
   float gx = 0.f, gy = 0.f, gz = 0.f, gs = 0.f;
   float ga[kMaxAttr];
 #pragma unroll
@@ -136,10 +149,12 @@ __global__ void __launch_bounds__(128) grad_kernel(Grid g, int b, Rbf r, int N, 
     for (int j = 0; j < cnt; ++j) {
       const float* e = sm + j * stride;
       const float x = e[0], y = e[1], z = e[2];
-      const float w = gaussian(x, y, z, xr, yr, zr, sigma);
-      const float d2 = (xr - x) * (xr - x) + (yr - y) * (yr - y) + (zr - z) * (zr - z);
-      const float dwx = (x - xr) * is2 * w, dwy = (y - yr) * is2 * w, dwz = (z - zr) * is2 * w;
-      const float dws = d2 * is2 / sigma * w;
+      const float ex = x - xr, ey = y - yr, ez = z - zr;
+      const float d2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+      const float w = exp2_approx(d2 * k2);
+      const float wi = is2 * w;
+      const float dwx = ex * wi, dwy = ey * wi, dwz = ez * wi;
+      const float dws = d2 * is3 * w;
       float dl = e[4 + 1 + A];
       if (A > 0) {
         float v0 = e[4];
