@@ -199,13 +199,15 @@ __global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
       }
     __syncthreads();
     if (inside) {
+      // one unsigned compare accepts a staged row (the window lies in [0, T));
+      // anything else is read from global memory if it is a bin at all
+      const unsigned srows = staged ? (unsigned)rows : 0u;
       for (int j = 0; j < cnt; ++j) {
         const float4 q = pts[j];
         const int t = velten_bin(mkv(q.x, q.y, q.z), q.w, p, bw, bo, fb);
-        if (t < 0 || t >= T) continue;
-        const int r = t - tlo;
-        value += (staged && r >= 0 && r < rows) ? win[r * (kST + 1) + j]
-                                                : __ldg(trb + (size_t)t * S + s0 + j);
+        const unsigned r = (unsigned)t - (unsigned)tlo;
+        if (r < srows) value += win[r * (kST + 1) + j];
+        else if ((unsigned)t < (unsigned)T) value += __ldg(trb + (size_t)t * S + s0 + j);
       }
     }
   }

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "capi_common.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace volume {
@@ -23,6 +24,7 @@ struct Geo {
   float scale;  // Z / sz
   float bw, bo;
   int T;
+  int exact;  // 1: every sample takes the exact chain (tuning key "volume.exact")
 };
 
 // Column / slice centre: origin + ((i + 0.5) * size) / n (volume_cuda.cu:35,38).
@@ -55,6 +57,43 @@ __device__ __forceinline__ Sample sample(const Geo& g, float wx, float wy, float
   s.zi = (int)fl;
   s.alpha = zh - fl;
   const float q = depth / (tc * tc);
+  s.f2 = (q * q) * (q * q);
+  return s;
+}
+
+// sample() with a filtered fast path: the depth from the hardware reciprocal
+// square root (within 6 u of the exact root, u = 2^-24) and z_hat from one
+// fused multiply-add. Against the exact chain z_hat moves by at most
+// scale 8 u (depth + |z| + |oz|) + 4 u |z_hat|, so where its fraction is
+// farther than that (with |wz| added) from 0 and 1 the fast floor is the
+// exact floor and the sample is kept; otherwise the exact sample() runs. The
+// d2 > 0 test is taken on the exact d2 either way. alpha and f2 are values
+// (few-ulp differences); every decision is the exact chain's. Used by the
+// adjoint (247 -> 195 ms on 128^3 x 16384 points x 1024 bins); the forward,
+// which only walks bins next to each occupied voxel's cell, ran 5% slower
+// with it and keeps sample().
+__device__ __forceinline__ Sample sample_filtered(const Geo& g, float wx, float wy, float wz,
+                                                  int t, float x, float y) {
+  if (g.exact) return sample(g, wx, wy, wz, t, x, y);
+  Sample s{false, 0, 0.f, 0.f};
+  const float tc = xadd(xmul((float)t, g.bw), g.bo);
+  const float dx = xsub(wx, x), dy = xsub(wy, y);
+  const float d2 = xsub(xsub(xmul(tc, tc), xmul(dx, dx)), xmul(dy, dy));
+  if (!(d2 > 0.f)) return s;
+  const float depth = d2 * rsqrtf(d2);
+  const float z = wz + depth;
+  const float zh = fmaf(z - g.oz, g.scale, -0.5f);
+  const float fl = floorf(zh);
+  const float fr = zh - fl;
+  const float u = 5.9604645e-8f;
+  const float m = 8.f * u * g.scale * (depth + fabsf(wz) + fabsf(z) + fabsf(g.oz)) +
+                  4.f * u * fabsf(zh) + 1e-7f;
+  if (!(fr > m && fr < 1.f - m)) return sample(g, wx, wy, wz, t, x, y);
+  if (!(fl >= 0.f && fl + 1.f < (float)g.Z)) return s;
+  s.ok = true;
+  s.zi = (int)fl;
+  s.alpha = fr;
+  const float q = __fdividef(depth, tc * tc);
   s.f2 = (q * q) * (q * q);
   return s;
 }
@@ -228,7 +267,7 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
     bin_range(g, rho2, wz, g.Z - 1, u0, u1);
     const float* row = tr + (size_t)i * g.T;
     for (int t = t0; t <= u1; ++t) {
-      const Sample s = sample(g, wx, wy, wz, t, x, y);
+      const Sample s = sample_filtered(g, wx, wy, wz, t, x, y);
       if (!s.ok) continue;
       const float v = __ldg(row + t) * s.f2;
       atomicAdd(col + s.zi, (1.f - s.alpha) * v);
@@ -318,6 +357,7 @@ Geo make_geo(int X, int Y, int Z, const float* o, const float* s, float bw, floa
   g.bw = bw;
   g.bo = bo;
   g.T = T;
+  g.exact = tune::get("volume.exact") == 1;
   return g;
 }
 
