@@ -80,6 +80,22 @@ __device__ __forceinline__ int velten_bin(fv3 q, float od2, fv3 p, float bw, flo
   return nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, p)))), bw, bo);
 }
 
+// velten_bin with the +1/2 folded into the offset (one rounding less, inside
+// the same error bound) and a margin m that bounds the per-pair margin of
+// velten_bin for every pair it is used on (the tiled kernel computes one per
+// tile from the distance and bin bounds of its voxel block).
+__device__ __forceinline__ int velten_bin_m(fv3 q, float od2, fv3 p, float bw, float bo,
+                                            float inv_bw, float nbo_half, float m) {
+  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float dist = fmaf(2.f, d2 * rsqrtf(d2), od2);
+  const float c = fmaf(dist, inv_bw, nbo_half);
+  const float t = floorf(c);
+  const float fr = c - t;
+  if (fr > m && fr < 1.f - m && fabsf(t) < 1.0e9f) return (int)t;
+  return nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, p)))), bw, bo);
+}
+
 struct Pts3 {  // [B, n, 3] with strides
   const float* p;
   int64_t sb, sn, sc;
@@ -141,6 +157,7 @@ __global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
   __shared__ float win[kWinRows * (kST + 1)];
   __shared__ float4 pts[kST];
   __shared__ int span[2];
+  __shared__ float tile_margin;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x0 = blockIdx.x * kBX, y0 = blockIdx.y * kBY, z0 = blockIdx.z * kBZ;
   const int x = x0 + (threadIdx.x & 7), y = y0 + ((threadIdx.x >> 3) & 7),
@@ -160,6 +177,7 @@ __global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
     __syncthreads();  // the previous tile is consumed
     if (warp == 0) {
       int tlo = INT_MAX, thi = INT_MIN;
+      float mrg = 0.f;  // margin bound of this lane's pairs (infinite: exact chain)
       if (lane < cnt) {
         const fv3 q = sp.at(b, s0 + lane);
         const float od2 = xmul(2.f, has_origin ? xlen(xsub3(q, so.at(b, s0 + lane))) : 0.f);
@@ -176,14 +194,22 @@ __global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
           tlo = max((int)floorf(fmaxf(cmin, -2.f)) - 1, 0);
           thi = min((int)floorf(fminf(cmax, (float)T + 2.f)) + 1, T - 1);
         }
+        // velten_bin's margin k1 dist + k2 + 1e-6 |c| at the largest distance
+        // and |c| of the block (2% slack for the rounding of these bounds)
+        const float dmax = fmaf(cmax - 0.5f, bw, bo);
+        const float cabs = fmaxf(fabsf(cmin), fabsf(cmax));
+        mrg = 1.02f * (fmaf(fb.k1, fabsf(dmax), fb.k2) + 1e-6f * cabs);
+        if (!(mrg == mrg)) mrg = INFINITY;
       }
       for (int o = 16; o > 0; o >>= 1) {
         tlo = min(tlo, __shfl_xor_sync(0xffffffffu, tlo, o));
         thi = max(thi, __shfl_xor_sync(0xffffffffu, thi, o));
+        mrg = fmaxf(mrg, __shfl_xor_sync(0xffffffffu, mrg, o));
       }
       if (lane == 0) {
         span[0] = tlo;
         span[1] = thi;
+        tile_margin = mrg;
       }
     }
     __syncthreads();
@@ -202,9 +228,11 @@ __global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
       // one unsigned compare accepts a staged row (the window lies in [0, T));
       // anything else is read from global memory if it is a bin at all
       const unsigned srows = staged ? (unsigned)rows : 0u;
+      const float m = tile_margin;
+      const float nbo_half = fb.nbo + 0.5f;
       for (int j = 0; j < cnt; ++j) {
         const float4 q = pts[j];
-        const int t = velten_bin(mkv(q.x, q.y, q.z), q.w, p, bw, bo, fb);
+        const int t = velten_bin_m(mkv(q.x, q.y, q.z), q.w, p, bw, bo, fb.inv_bw, nbo_half, m);
         const unsigned r = (unsigned)t - (unsigned)tlo;
         if (r < srows) value += win[r * (kST + 1) + j];
         else if ((unsigned)t < (unsigned)T) value += __ldg(trb + (size_t)t * S + s0 + j);
