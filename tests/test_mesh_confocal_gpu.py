@@ -214,3 +214,50 @@ def test_filtered_fast_path_keeps_exact_bins(cuda_lib):
     # the gradient takes the exact chain either way (atomic order only)
     assert rel_l2(va.numpy(), vb.numpy()) < 1e-5
     assert rel_l2(ma.numpy(), mb.numpy()) < 1e-5
+
+
+@pytest.mark.parametrize("ts", [1, 4, 8, 16])
+def test_compact_splat_matches_pair_per_thread(cuda_lib, ts):
+    """The compacted splat (visible pairs queued per warp) sums the same
+    contributions as the pair-per-thread splat, at every scan tile width; only
+    the order of the shared-memory atomics differs. The small scene with
+    padded faces checks it against the FP64 oracle as well."""
+    from totri_gb300 import autotune
+    s = scenes.confocal_differentiable()
+    d = _dev(s)
+    bd = s["bin_def"]
+    empty = torch.empty_like(d["scan_points"][:, :0])
+    out = []
+    for mode in (0, 1):
+        autotune.set_tile("mesh.confocal.splat.mode", mode)
+        autotune.set_tile("mesh.confocal.splat.ts", ts)
+        try:
+            tr = torch.empty((1, bd.num, d["scan_points"].shape[1]), device="cuda")
+            R.mesh_confocal_forward(d["verts"], d["faces"], d["colors"], d["scan_points"], empty,
+                                    tr, bd.width, bd.offset, 0)
+            out.append(tr.cpu().numpy())
+        finally:
+            autotune.set_tile("mesh.confocal.splat.mode", 0)
+            autotune.set_tile("mesh.confocal.splat.ts", 0)
+    assert rel_l2(out[1], out[0]) < 1e-6
+    assert np.array_equal(out[1] == 0, out[0] == 0)
+
+    sm = scenes.confocal_small(seed=6)
+    n = np_scene(sm)
+    bd = sm["bin_def"]
+    ds = _dev(sm)
+    ds["faces"][0, 201, 2] = -1  # the list ends at face 201, inside a 32-face chunk
+    n["faces"] = ds["faces"][0].cpu().numpy()
+    vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    ref = _oracle_forward(n, vis, bd)
+    autotune.set_tile("mesh.confocal.splat.mode", 1)
+    autotune.set_tile("mesh.confocal.splat.ts", ts)
+    try:
+        tr = torch.empty((1, bd.num, n["scan_points"].shape[0]), device="cuda")
+        R.mesh_confocal_forward(ds["verts"], ds["faces"], ds["colors"], ds["scan_points"],
+                                torch.empty_like(ds["scan_points"][:, :0]), tr, bd.width,
+                                bd.offset, 0)
+    finally:
+        autotune.set_tile("mesh.confocal.splat.mode", 0)
+        autotune.set_tile("mesh.confocal.splat.ts", 0)
+    assert rel_l2(tr[0].double().cpu().numpy(), ref) < FWD_TOL

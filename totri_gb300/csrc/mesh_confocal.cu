@@ -228,6 +228,93 @@ __global__ void __launch_bounds__(256) splat_kernel(Scene sc, View3f sp, View3f 
   flush_tile<TS>(hist, transient + (size_t)b * T * S, T, S, s0);
 }
 
+// splat_kernel with the visible pairs compacted first: each warp walks
+// 32-face chunks (lane = face), gathers each face's visibility over the TS
+// scan points of the tile, queues the visible (face, point) pairs in shared
+// memory and evaluates them 32 at a time, one per lane, instead of leaving the
+// lanes of occluded pairs idle. A face hands out its points starting at a
+// lane-dependent offset, so the 32 pairs of a batch fall on different
+// histogram columns and their shared atomics seldom collide.
+template <int TS>
+__global__ void __launch_bounds__(256, 2) splat_compact_kernel(Scene sc, View3f sp, View3f so,
+                                                            int has_origin,
+                                                            float* __restrict__ transient, int T,
+                                                            int S, float bw, float bo,
+                                                            FastBins fb) {
+  extern __shared__ float hist[];  // [T][TS]
+  __shared__ float pts[TS][4];     // scan point, 2 |scan - origin|
+  __shared__ int queue[8][64];
+  const int b = blockIdx.y;
+  const int s0 = blockIdx.x * TS;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < T * TS; i += blockDim.x) hist[i] = 0.f;
+  if (threadIdx.x < TS && s0 + (int)threadIdx.x < S) {
+    const int s = s0 + threadIdx.x;
+    const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+    pts[threadIdx.x][0] = p.x;
+    pts[threadIdx.x][1] = p.y;
+    pts[threadIdx.x][2] = p.z;
+    pts[threadIdx.x][3] =
+        has_origin ? xmul(2.f, xlen(xsub3(p, mkv(so.at(b, s, 0), so.at(b, s, 1), so.at(b, s, 2)))))
+                   : 0.f;
+  }
+  __syncthreads();
+  const int n = sc.meta[b].n;
+  const int nchu = (n + 31) >> 5;
+  const int ts = min(TS, S - s0);
+  const uint32_t* m0 = sc.mask + ((size_t)b * sc.P + s0) * sc.nch;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  const uint32_t below = (1u << lane) - 1u;
+  int* qw = queue[warp];
+  int cnt = 0;  // warp-uniform
+  auto run = [&](int e) {
+    const int k = e >> 4, sl = e & 15;
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 p = mkv(pts[sl][0], pts[sl][1], pts[sl][2]);
+    ConfocalPair q;
+    confocal_pair_filtered(s0r, s1r, s2r, p, pts[sl][3], bw, bo, fb, q);
+    const float alpha = alpha_confocal(q, mkv(s3r.x, s3r.y, s3r.z), p, s0r.w);
+    if (!(alpha > 0.f)) return;
+    const Hist<TS> h{hist, sl, T};
+    splat_tent(h, q.c, q.bin, alpha);
+  };
+  const int rot = lane & (TS - 1);
+  for (int ch = warp; ch < nchu; ch += 8) {
+    const uint32_t w = lane < ts ? __ldg(m0 + (size_t)lane * sc.nch + ch) : 0u;
+    // vm: this lane's face, bit sl = visible from scan point s0 + sl; faces
+    // at or past n never count, whatever the mask words hold there.
+    uint32_t vm = 0u;
+    for (int sl = 0; sl < ts; ++sl) vm |= ((__shfl_sync(0xffffffffu, w, sl) >> lane) & 1u) << sl;
+    if (ch * 32 + lane >= n) vm = 0u;
+    while (__any_sync(0xffffffffu, vm != 0u)) {
+      const bool has = vm != 0u;
+      int sl = 0;
+      if (has) {  // next visible point, counting from this lane's offset
+        const uint32_t r = ((vm >> rot) | (vm << ((TS - rot) & 31))) & ((1u << TS) - 1u);
+        sl = (__ffs(r) - 1 + rot) & (TS - 1);
+        vm &= ~(1u << sl);
+      }
+      const uint32_t take = __ballot_sync(0xffffffffu, has);
+      if (has) qw[cnt + __popc(take & below)] = ((ch * 32 + lane) << 4) | sl;
+      cnt += __popc(take);  // below 64: at most 31 queued before, 32 added
+      if (cnt >= 32) {
+        __syncwarp();
+        const int e = qw[lane];
+        __syncwarp();
+        if (lane < cnt - 32) qw[lane] = qw[32 + lane];
+        cnt -= 32;
+        __syncwarp();
+        run(e);
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < cnt) run(qw[lane]);
+  __syncthreads();
+  flush_tile<TS>(hist, transient + (size_t)b * T * S, T, S, s0);
+}
+
 // Gradient of one visible pair with respect to the three (sorted) vertices and
 // the albedo, following mesh_confocal_grad_verts_optix.cu:248-314 and
 // AlphaConfocalGradVerts (mesh_common.h:429-463). Returns false when the pair
@@ -413,13 +500,26 @@ static int launch_splat_ts(const Scene& sc, const View3f& sp, const View3f& so, 
                            float* transient, int T, int S, float bw, float bo,
                            cudaStream_t stream) {
   const size_t smem = sizeof(float) * (size_t)T * TS;
+  const dim3 grid((unsigned)ceil_div(S, TS), (unsigned)sc.B);
+  if (tune::get("mesh.confocal.splat.mode") == 1) {
+    static int configured_c = 0;
+    if (smem > 40 * 1024 && configured_c < (int)smem) {  // 2.3 KB static shared memory besides
+      TOTRI_CUDA(cudaFuncSetAttribute(splat_compact_kernel<TS>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      configured_c = (int)smem;
+    }
+    TOTRI_KERNEL("mesh confocal splat", stream,
+                 splat_compact_kernel<TS><<<grid, 256, smem, stream>>>(
+                     sc, sp, so, has_origin, transient, T, S, bw, bo,
+                     make_fast_bins(bw, bo, tune::get("mesh.confocal.exact") != 1)));
+    return TOTRI_OK;
+  }
   static int configured = 0;
   if (smem > 48 * 1024 && configured < (int)smem) {
     TOTRI_CUDA(cudaFuncSetAttribute(splat_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
     configured = (int)smem;
   }
-  const dim3 grid((unsigned)ceil_div(S, TS), (unsigned)sc.B);
   TOTRI_KERNEL("mesh confocal splat", stream,
                splat_kernel<TS><<<grid, 256, smem, stream>>>(
                    sc, sp, so, has_origin, transient, T, S, bw, bo,
