@@ -261,3 +261,59 @@ def test_compact_splat_matches_pair_per_thread(cuda_lib, ts):
         autotune.set_tile("mesh.confocal.splat.mode", 0)
         autotune.set_tile("mesh.confocal.splat.ts", 0)
     assert rel_l2(tr[0].double().cpu().numpy(), ref) < FWD_TOL
+
+
+_SEED_CASES = [  # (mesh.visibility.seed, mesh.visibility.seed.steps, mesh.visibility.chunks)
+    (1, 0, 0),   # surface walk off
+    (0, 0, 0),   # defaults: faces seen from behind, 48 steps, chunks by grid size
+    (2, 4, 3),   # every target, short walks, 3 chunks per block
+    (3, 64, 16),
+    (0, 1, 1),
+]
+
+
+def _with_seed(case, fn):
+    from totri_gb300 import autotune
+    keys = ("mesh.visibility.seed", "mesh.visibility.seed.steps", "mesh.visibility.chunks")
+    for k, v in zip(keys, case):
+        autotune.set_tile(k, v)
+    try:
+        return fn()
+    finally:
+        for k in keys:
+            autotune.set_tile(k, 0)
+
+
+def test_seeded_visibility_equals_brute_force(cuda_lib):
+    """The surface walk from the last occluder of each wall point can only
+    prove 'not visible' with the exact leaf test, so the masks equal the
+    brute-force masks bit for bit whatever the walk's settings; full-size
+    20,480-face workload."""
+    s = scenes.confocal_differentiable()
+    d = _dev(s)
+    bf = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
+    for case in _SEED_CASES:
+        got = _with_seed(case, lambda: R.mesh_visibility(d["verts"], d["faces"],
+                                                         d["scan_points"]))
+        assert torch.equal(got, bf), case
+
+
+def test_seeded_visibility_without_or_with_odd_adjacency(cuda_lib):
+    """Edge adjacency only steers the walk: a triangle soup (no shared vertex
+    indices), non-manifold fins (three faces on one edge) and degenerate faces
+    leave the masks equal to the oracle's."""
+    s = scenes.confocal_small(seed=4)
+    v, f = s["verts"][0], s["faces"][0]
+    soup_v = v[f.reshape(-1).long()].reshape(1, -1, 3).contiguous()
+    soup_f = torch.arange(soup_v.shape[1], dtype=f.dtype).reshape(1, -1, 3)
+    fins = torch.stack([f[:40, 0], f[:40, 1], f[40:80, 2]], 1)  # reuse edges of 40 faces
+    degen = torch.stack([f[80:90, 0], f[80:90, 0], f[80:90, 1]], 1)
+    odd_f = torch.cat([f, fins, degen])[None].contiguous()
+    pts = s["scan_points"]
+    for verts, faces in ((soup_v, soup_f), (v[None].contiguous(), odd_f)):
+        ref = oracle.mesh_visibility(verts[0].numpy(), faces[0].numpy(), pts[0].numpy())
+        F = faces.shape[1]
+        for case in _SEED_CASES:
+            got = _with_seed(case, lambda: R.mesh_visibility(verts.cuda(), faces.cuda(),
+                                                             pts.cuda()))
+            assert np.array_equal(unpack_mask(got[0].cpu().numpy(), F), ref), case

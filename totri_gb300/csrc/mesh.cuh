@@ -27,6 +27,8 @@ namespace mesh {
 //           original vertices, FP32 centroid, vertex indices.
 // Node:     (lo0.xyz, hi0.x) (hi0.yz, lo1.xy) (lo1.z, hi1.xyz) (c0, c1, -, -)
 //           child >= 0: internal node, child < 0: leaf ~child.
+// Adj:      int4 (a0, a1, a2, -): a_e = Morton position of the face sharing
+//           the edge opposite vertex e (vertex indices compared), -1 if none.
 
 struct Meta {
   int n;          // faces before the first invalid one
@@ -55,6 +57,10 @@ struct Scene {
   int* counter;    // [B][F]
   uint32_t* mask;  // [B][P][nch]
   uint32_t* pscratch;  // [4][B][P]: wall-point sort keys/values (ping-pong)
+  int4* adj;       // [B][F] edge neighbours (Adj)
+  unsigned long long* ekeys;  // [B][ecap] edge hash keys (build scratch)
+  int2* evals;     // [B][ecap] the first two faces holding each edge
+  int ecap;        // edge hash capacity per item (4 F)
   uint32_t* status;
   int sorted_buf;  // which ping-pong half holds the sorted keys (0/1)
 };
@@ -71,8 +77,8 @@ struct BuildInputs {
 
 // Workspace layout on the host.
 struct Layout {
-  size_t header, meta, keys, vals, tri, shade, nodes, wide, lparent, iparent, counter, mask,
-      pscratch, total;
+  size_t header, meta, keys, vals, tri, shade, nodes, wide, lparent, iparent, counter, adj,
+      ekeys, evals, mask, pscratch, total;
 };
 
 inline Layout layout(int64_t B, int64_t F, int64_t P) {
@@ -96,6 +102,9 @@ inline Layout layout(int64_t B, int64_t F, int64_t P) {
   L.lparent = take(sizeof(int) * B * Fc);
   L.iparent = take(sizeof(int) * B * Fc);
   L.counter = take(sizeof(int) * B * Fc);
+  L.adj = take(sizeof(int4) * B * Fc);
+  L.ekeys = take(sizeof(unsigned long long) * B * 4 * Fc);
+  L.evals = take(sizeof(int2) * B * 4 * Fc);
   L.mask = take(sizeof(uint32_t) * B * P * nch);
   L.pscratch = take(sizeof(uint32_t) * 4 * B * P);
   L.total = off;
@@ -121,6 +130,10 @@ inline Scene scene_from_workspace(void* ws, int64_t B, int64_t F, int64_t P) {
   s.lparent = reinterpret_cast<int*>(base + L.lparent);
   s.iparent = reinterpret_cast<int*>(base + L.iparent);
   s.counter = reinterpret_cast<int*>(base + L.counter);
+  s.adj = reinterpret_cast<int4*>(base + L.adj);
+  s.ekeys = reinterpret_cast<unsigned long long*>(base + L.ekeys);
+  s.evals = reinterpret_cast<int2*>(base + L.evals);
+  s.ecap = 4 * s.F;
   s.mask = reinterpret_cast<uint32_t*>(base + L.mask);
   s.pscratch = reinterpret_cast<uint32_t*>(base + L.pscratch);
   s.sorted_buf = 1;  // three 10-bit radix passes end in the second half
@@ -178,6 +191,40 @@ __device__ __forceinline__ bool tri_hit(float4 t0, float4 t1, float4 t2, float4 
   if (!(u >= 0.f && u <= 1.f)) return false;
   const fv3 q = xcross(tv, e1);
   const float v = xmul(xdot(d, q), inv);
+  if (!(v >= 0.f && xadd(u, v) <= 1.f)) return false;
+  const float t = xmul(xdot(e2, q), inv);
+  if (!(t >= 0.f && t <= tmax)) return false;
+  const float px = xfma(t, d.x, o.x);
+  const float py = xfma(t, d.y, o.y);
+  const float pz = xfma(t, d.z, o.z);
+  if (!(px >= t2.y && px <= t3.x && py >= t2.z && py <= t3.y && pz >= t2.w && pz <= t3.z))
+    return false;
+  tout = t;
+  return true;
+}
+
+// tri_hit that also returns the barycentric coordinates (u, v) of the ray's
+// crossing with the face's plane, computed where tri_hit stops early as well.
+// The decision and t are tri_hit's: the same operations in the same order.
+__device__ __forceinline__ bool tri_hit_uv(float4 t0, float4 t1, float4 t2, float4 t3, fv3 o,
+                                           fv3 d, float tmax, float& tout, float& uo,
+                                           float& vo) {
+  const fv3 v0 = mkv(t0.x, t0.y, t0.z);
+  const fv3 e1 = mkv(t0.w, t1.x, t1.y);
+  const fv3 e2 = mkv(t1.z, t1.w, t2.x);
+  const fv3 p = xcross(d, e2);
+  const float det = xdot(e1, p);
+  uo = 0.f;
+  vo = 0.f;
+  if (det == 0.f) return false;
+  const float inv = xrcp(det);
+  const fv3 tv = xsub3(o, v0);
+  const float u = xmul(xdot(tv, p), inv);
+  const fv3 q = xcross(tv, e1);
+  const float v = xmul(xdot(d, q), inv);
+  uo = u;
+  vo = v;
+  if (!(u >= 0.f && u <= 1.f)) return false;
   if (!(v >= 0.f && xadd(u, v) <= 1.f)) return false;
   const float t = xmul(xdot(e2, q), inv);
   if (!(t >= 0.f && t <= tmax)) return false;
@@ -314,14 +361,64 @@ __device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, 
   return true;
 }
 
+// Which targets try the surface walk first (the value of the tuning key
+// mesh.visibility.seed; 0, the default, takes the faces seen from behind).
+enum SeedMode { kSeedBack = 0, kSeedOff = 1, kSeedAll = 2, kSeedFront = 3 };
+
+// Surface walk: a search for an occluder of the ray from o to target k that
+// starts at face g (the occluder found for a neighbouring query) and moves
+// across the mesh's edges. Each face is tested exactly as the BVH walk tests a
+// leaf; a face that does not occlude hands over to its neighbour beyond the
+// edge that the ray's crossing with its plane lies outside of (the most
+// negative barycentric coordinate). The walk stops at the target, at a mesh
+// boundary, where the crossing lies inside the face, or after `steps` faces.
+// It returns an occluder's Morton position or -1; it can only prove "not
+// visible", so a wrong turn costs time, never a mask bit.
+__device__ __forceinline__ int surface_walk(const Scene& sc, int b, int n, int k, int f, int g,
+                                            fv3 o, fv3 dir, float tmax, float tf, int steps) {
+  const float4* tri = sc.tri + (size_t)b * sc.F * 4;
+  const int4* adj = sc.adj + (size_t)b * sc.F;
+  for (int st = 0; st < steps; ++st) {
+    if (g == k || (unsigned)g >= (unsigned)n) return -1;
+    const float4* q = tri + (size_t)g * 4;
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+    float tq, u, v;
+    if (tri_hit_uv(q0, q1, q2, q3, o, dir, tmax, tq, u, v) &&
+        (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
+      return g;
+    const float w0 = 1.f - u - v;
+    int e;
+    float wm;
+    if (w0 <= u && w0 <= v) {
+      e = 0;
+      wm = w0;
+    } else if (u <= v) {
+      e = 1;
+      wm = u;
+    } else {
+      e = 2;
+      wm = v;
+    }
+    if (!(wm < 0.f)) return -1;
+    const int4 a = __ldg(adj + g);
+    g = e == 0 ? a.x : (e == 1 ? a.y : a.z);
+    if (g < 0) return -1;
+  }
+  return -1;
+}
+
 // target_visible with postponed leaf tests (the "while-while" organisation
 // of Aila and Laine, HPG 2009): a lane that reaches a leaf parks it and keeps
 // walking internal nodes until no lane of the warp still walking lacks a
 // parked leaf; the triangle tests, the costliest step of the walk, then run
 // together. The leaves tested, and so the answer, are those of
 // target_visible (any occluder settles the ray; order does not matter).
+// With seed_steps > 0 and a seed face (seed >= 0), the targets that seed_mode
+// selects first try surface_walk from the seed; `seed` returns the occluder
+// found by either search, for the next query.
 __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
-                                                  const Target& tg, fv3 o, uint32_t* status) {
+                                                  const Target& tg, fv3 o, uint32_t* status,
+                                                  int& seed, int seed_mode, int seed_steps) {
   constexpr int kDone = INT_MIN;  // below every leaf code ~k, k < n
   const int k = tg.k;
   const fv3 D = xsub3(tg.c, o);
@@ -333,6 +430,20 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
   float tf;
   if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return false;
   if (n == 1) return true;
+  if (seed_steps > 0 && seed >= 0 && seed_mode != kSeedOff) {
+    bool walk = seed_mode == kSeedAll;
+    if (!walk) {  // faces wound outward and seen from behind are mostly occluded
+      const fv3 nrm = cross(mkv(tg.a0.w, tg.a1.x, tg.a1.y), mkv(tg.a1.z, tg.a1.w, tg.a2.x));
+      walk = (dot(nrm, D) > 0.f) == (seed_mode == kSeedBack);
+    }
+    if (walk) {
+      const int g = surface_walk(sc, b, n, k, f, seed, o, dir, tmax, tf, seed_steps);
+      if (g >= 0) {
+        seed = g;
+        return false;
+      }
+    }
+  }
   const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
   const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   int stack[64];
@@ -383,8 +494,10 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
           const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
           float tq;
           if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
-              (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
+              (tq < tf || (tq == tf && __float_as_int(q3.w) < f))) {
+            seed = kk;
             return false;
+          }
         }
       }
       leaf = kDone;

@@ -239,7 +239,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_kernel(Scene sc) {
 
 // Morton order of P wall points, one CTA per batch item: bounding box, 30-bit
 // codes over it, radix sort. scr is [4][B][P] (keys, values, keys, values);
-// the permutation (point indices in Morton order) ends in the fourth quarter.
+// the permutation (point indices in Morton order) ends in the fourth quarter,
+// and the first quarter is then set to -1: the visibility kernel keeps each
+// point's last occluder there (by Morton position of the point).
 __global__ void __launch_bounds__(kSortThreads) point_order_kernel(View3f pts, int P, int B,
                                                                   uint32_t* scr) {
   extern __shared__ uint32_t smem[];
@@ -281,6 +283,8 @@ __global__ void __launch_bounds__(kSortThreads) point_order_kernel(View3f pts, i
   }
   __syncthreads();
   cta_radix_sort30(k0, v0, k1, v1, P, smem);
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) k0[i] = ~0u;
 }
 
 __global__ void records_kernel(Scene sc, BuildInputs in) {
@@ -434,6 +438,84 @@ __global__ void widen_kernel(Scene sc) {
   w[7] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Edge adjacency of the valid faces, in Morton positions. Each face inserts
+// its three edges (the unordered pair of vertex indices) into an
+// open-addressing hash table of 4 F slots per item; a slot keeps the first two
+// faces that hold its edge. Adjacency only steers the surface walk that seeds
+// the visibility query with likely occluders: it never decides a mask bit, so
+// non-manifold edges (a third face is left out), seams with duplicated
+// vertices (no neighbour) and degenerate faces cost speed, not exactness.
+constexpr unsigned long long kEdgeEmpty = ~0ull;
+
+__device__ __forceinline__ unsigned long long edge_key(uint32_t a, uint32_t c) {
+  return a < c ? ((unsigned long long)a << 32) | c : ((unsigned long long)c << 32) | a;
+}
+
+__device__ __forceinline__ int edge_slot(unsigned long long key, int cap) {
+  return (int)(((key * 0x9E3779B97F4A7C15ull) >> 32) % (unsigned long long)cap);
+}
+
+__device__ __forceinline__ void face_vertex_ids(const Scene& sc, int b, int k, uint32_t vi[3]) {
+  const float4* s = sc.shade + ((size_t)b * sc.F + k) * 4;
+  vi[0] = (uint32_t)__float_as_int(s[1].w);
+  vi[1] = (uint32_t)__float_as_int(s[2].w);
+  vi[2] = (uint32_t)__float_as_int(s[3].w);
+}
+
+__global__ void edge_insert_kernel(Scene sc) {
+  const int b = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sc.meta[b].n) return;
+  uint32_t vi[3];
+  face_vertex_ids(sc, b, k, vi);
+  unsigned long long* keys = sc.ekeys + (size_t)b * sc.ecap;
+  int2* vals = sc.evals + (size_t)b * sc.ecap;
+  for (int e = 0; e < 3; ++e) {
+    const uint32_t a = vi[(e + 1) % 3], c = vi[(e + 2) % 3];
+    if (a == c) continue;
+    const unsigned long long key = edge_key(a, c);
+    int h = edge_slot(key, sc.ecap);
+    for (int it = 0; it < sc.ecap; ++it) {  // 3 n <= 3 F keys in 4 F slots: a slot is found
+      const unsigned long long prev = atomicCAS(&keys[h], kEdgeEmpty, key);
+      if (prev == kEdgeEmpty || prev == key) {
+        if (atomicCAS(&vals[h].x, -1, k) != -1) atomicCAS(&vals[h].y, -1, k);
+        break;
+      }
+      h = h + 1 == sc.ecap ? 0 : h + 1;
+    }
+  }
+}
+
+__global__ void edge_link_kernel(Scene sc) {
+  const int b = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sc.meta[b].n) return;
+  uint32_t vi[3];
+  face_vertex_ids(sc, b, k, vi);
+  const unsigned long long* keys = sc.ekeys + (size_t)b * sc.ecap;
+  const int2* vals = sc.evals + (size_t)b * sc.ecap;
+  int nb[3];
+  for (int e = 0; e < 3; ++e) {
+    nb[e] = -1;
+    const uint32_t a = vi[(e + 1) % 3], c = vi[(e + 2) % 3];
+    if (a == c) continue;
+    const unsigned long long key = edge_key(a, c);
+    int h = edge_slot(key, sc.ecap);
+    for (int it = 0; it < sc.ecap; ++it) {
+      const unsigned long long kk = keys[h];
+      if (kk == key) {
+        const int2 v = vals[h];
+        nb[e] = v.x == k ? v.y : v.x;
+        break;
+      }
+      if (kk == kEdgeEmpty) break;
+      h = h + 1 == sc.ecap ? 0 : h + 1;
+    }
+    if (nb[e] == k) nb[e] = -1;
+  }
+  sc.adj[(size_t)b * sc.F + k] = make_int4(nb[0], nb[1], nb[2], 0);
+}
+
 int launch_point_order(const Scene& sc, const View3f& pts, int P, cudaStream_t stream) {
   const size_t smem = sizeof(uint32_t) * (32 * kSortDigits + 2 * kSortDigits);
   static bool attr_set = false;
@@ -467,6 +549,10 @@ int build_scene(const Scene& sc, const BuildInputs& in, cudaStream_t stream) {
     }
     TOTRI_KERNEL("mesh sort", stream, sort_kernel<<<B, kSortThreads, smem, stream>>>(sc));
     TOTRI_KERNEL("mesh records", stream, records_kernel<<<gridF, blk, 0, stream>>>(sc, in));
+    TOTRI_CUDA(cudaMemsetAsync(sc.ekeys, 0xff, sizeof(unsigned long long) * B * sc.ecap, stream));
+    TOTRI_CUDA(cudaMemsetAsync(sc.evals, 0xff, sizeof(int2) * B * sc.ecap, stream));
+    TOTRI_KERNEL("mesh edges", stream, edge_insert_kernel<<<gridF, blk, 0, stream>>>(sc));
+    TOTRI_KERNEL("mesh edges", stream, edge_link_kernel<<<gridF, blk, 0, stream>>>(sc));
     TOTRI_KERNEL("mesh hierarchy", stream, hierarchy_kernel<<<gridF, blk, 0, stream>>>(sc));
     TOTRI_KERNEL("mesh refit", stream, refit_kernel<<<gridF, blk, 0, stream>>>(sc));
     TOTRI_KERNEL("mesh widen", stream, widen_kernel<<<gridF, blk, 0, stream>>>(sc));

@@ -16,6 +16,8 @@
 //    keep every SM busy when there are few faces), keeps
 //    the per-face gradient in registers, reduces it across the warp and issues
 //    12 atomics per face instead of 9 + 3M per visible pair.
+#include <algorithm>
+
 #include "mesh.cuh"
 #include "mesh_kernels.cuh"
 #include "tune.cuh"
@@ -64,7 +66,9 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
       vis = packet_visible(sc, b, n, k < n, tg, o, sc.status);
     }
   } else if (kMode == kVisRayPostponed) {
-    if (k < n) vis = target_visible_pp(sc, b, n, load_target(sc, b, k), o, sc.status);
+    int seed = -1;
+    if (k < n) vis = target_visible_pp(sc, b, n, load_target(sc, b, k), o, sc.status, seed,
+                                       kSeedOff, 0);
   } else if (k < n) {
     int cache = -1;
     vis = target_visible<kMode == kVisBrute>(sc, b, n, load_target(sc, b, k), o, cache,
@@ -74,48 +78,78 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
   if (lane == 0) sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
 }
 
-// One CTA per (block of 32 wall points in Morton order, 32-face chunk): each
-// warp takes one face of the chunk at a time and its 32 lanes cast the rays
-// from the 32 points, which lie on a compact patch of the wall and end on the
-// same centroid, so the lanes walk nearly the same BVH nodes (lockstep model on
-// the 20,480-face sphere: 12% fewer warp iterations and 8.3 -> 5.7 distinct
-// nodes per iteration against point-major warps; measured 15.3 ms against
-// 22.6 ms for point-major warps with the same postponed-leaf walk). The eight
-// warps of a CTA work on neighbouring faces from the same points, so they share
-// their BVH nodes in L1 (a variant without the CTA, one warp per 32 x 32 block,
-// took 23.2 ms). The 32 x 32 bits are transposed in shared memory into one
-// mask word per point. This is the default visibility kernel.
+// One CTA per (block of 32 wall points in Morton order, run of `chunks`
+// 32-face chunks): for each chunk, each warp takes one face at a time and its
+// 32 lanes cast the rays from the 32 points, which lie on a compact patch of
+// the wall and end on the same centroid, so the lanes walk nearly the same BVH
+// nodes (lockstep model on the 20,480-face sphere: 12% fewer warp iterations
+// and 8.3 -> 5.7 distinct nodes per iteration against point-major warps;
+// measured 15.3 ms against 22.6 ms for point-major warps with the same
+// postponed-leaf walk). The eight warps of a CTA work on neighbouring faces
+// from the same points, so they share their BVH nodes in L1 (a variant
+// without the CTA, one warp per 32 x 32 block, took 23.2 ms).
+//
+// With the binary walk (kWalk 0) each point keeps a seed in shared memory: the
+// last occluder any warp of the CTA found for it. Faces of neighbouring Morton
+// positions are close on the surface, and so are the faces that hide them from
+// one wall point, so a short surface walk from the seed (surface_walk) settles
+// most hidden targets without a BVH walk. A CTA starts from the seeds that
+// earlier CTAs of the same points left in global memory (the first quarter of
+// the point scratch, -1 after the point sort) and leaves its own there. Seeds
+// are read and written without synchronisation, as any face is a valid (if
+// slower) start. The bits of every chunk are transposed in shared memory into
+// one mask word per point and chunk. This is the default visibility kernel.
+constexpr int kMaxPatchChunks = 16;
+
 template <int kWalk>  // 0: target_visible_pp, 1: packet_visible, 2: target_visible_pp4
 __global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f pts, int P,
-                                                               int row0) {
-  __shared__ uint32_t bits[32];  // face j of the chunk: visible from point lane
+                                                               int row0, int chunks,
+                                                               int seed_mode, int seed_steps) {
+  __shared__ uint32_t bits[kMaxPatchChunks][32];  // [chunk][face j]: visible from point lane
+  __shared__ int seeds[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int b = blockIdx.z;
-  const int ch = blockIdx.y;
+  const int ch0 = blockIdx.y * chunks;
   const int i = blockIdx.x * 32 + lane;  // position in Morton order
   const int n = sc.meta[b].n;
   const bool okp = i < P;
   const uint32_t* order = sc.pscratch + 3 * (size_t)sc.B * P + (size_t)b * P;
   const int p = okp ? (int)order[i] : 0;
   const fv3 o = okp ? mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2)) : mkv(0.f, 0.f, 0.f);
-  for (int j = warp; j < 32; j += 8) {
-    const int k = ch * 32 + j;
-    bool vis = false;
-    if (k < n) {  // warp-uniform
-      const Target tg = load_target(sc, b, k);
-      if (kWalk == 1) vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
-      else if (kWalk == 2) vis = okp && target_visible_pp4(sc, b, n, tg, o, sc.status);
-      else vis = okp && target_visible_pp(sc, b, n, tg, o, sc.status);
+  volatile int* vseeds = seeds;
+  volatile int* gseeds = reinterpret_cast<int*>(sc.pscratch) + (size_t)b * P;
+  if (threadIdx.x < 32) seeds[lane] = okp ? gseeds[i] : -1;
+  __syncthreads();
+  const int nc = min(chunks, sc.nch - ch0);
+  for (int c = 0; c < nc; ++c) {
+    for (int j = warp; j < 32; j += 8) {
+      const int k = (ch0 + c) * 32 + j;
+      bool vis = false;
+      if (k < n) {  // warp-uniform
+        const Target tg = load_target(sc, b, k);
+        if (kWalk == 1) {
+          vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
+        } else if (kWalk == 2) {
+          vis = okp && target_visible_pp4(sc, b, n, tg, o, sc.status);
+        } else if (okp) {
+          const int s0 = vseeds[lane];
+          int seed = s0;
+          vis = target_visible_pp(sc, b, n, tg, o, sc.status, seed, seed_mode, seed_steps);
+          if (seed != s0) vseeds[lane] = seed;
+        }
+      }
+      const uint32_t w = __ballot_sync(0xffffffffu, vis);
+      if (lane == 0) bits[c][j] = w;
     }
-    const uint32_t w = __ballot_sync(0xffffffffu, vis);
-    if (lane == 0) bits[j] = w;
   }
   __syncthreads();
-  if (threadIdx.x < 32 && okp) {
+  if (threadIdx.x < 32 && okp && kWalk == 0) gseeds[i] = seeds[lane];
+  for (int c = warp; c < nc; c += 8) {
+    if (!okp) continue;
     uint32_t word = 0u;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) word |= ((bits[j] >> lane) & 1u) << j;
-    sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch] = word;
+    for (int j = 0; j < 32; ++j) word |= ((bits[c][j] >> lane) & 1u) << j;
+    sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch0 + c] = word;
   }
 }
 
@@ -480,17 +514,35 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
     if (P >= (1 << 30) / 4) return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points");
     const int st = launch_point_order(sc, pts, P, stream);
     if (st != TOTRI_OK) return st;
-    const dim3 grid((unsigned)ceil_div(P, 32), (unsigned)sc.nch, (unsigned)sc.B);
+    // Chunks per CTA: 2 while the grid keeps 8 CTAs per SM (10.2 ms against
+    // 11.1 ms for 1 and 10.6 ms for 4 on the 20,480-face workload).
+    int chunks = tune::get("mesh.visibility.chunks");
+    if (chunks <= 0) {
+      const int64_t ctas = (int64_t)ceil_div(P, 32) * sc.nch * sc.B;
+      chunks = (int)std::max<int64_t>(1, std::min<int64_t>(2, ctas / (8 * tune::sm_count())));
+    }
+    if (chunks > kMaxPatchChunks)
+      return fail(TOTRI_ERR_INVALID_ARGUMENT, "at most 16 face chunks per visibility block");
+    const int seed_mode = tune::get("mesh.visibility.seed");
+    if (seed_mode < kSeedBack || seed_mode > kSeedFront)
+      return fail(TOTRI_ERR_INVALID_ARGUMENT, "visibility seed mode must be 0..3");
+    int seed_steps = tune::get("mesh.visibility.seed.steps");
+    if (seed_steps <= 0) seed_steps = 48;
+    const dim3 grid((unsigned)ceil_div(P, 32), (unsigned)ceil_div(sc.nch, chunks),
+                    (unsigned)sc.B);
     const int mode = tune::get("mesh.visibility.mode");
     if (mode == kVisPatchPacket)
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<1><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+                   visibility_patch_kernel<1><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, kSeedOff, 0));
     else if (mode == kVisPatchWide)
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<2><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+                   visibility_patch_kernel<2><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, kSeedOff, 0));
     else
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<0><<<grid, 256, 0, stream>>>(sc, pts, P, row0));
+                   visibility_patch_kernel<0><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, seed_mode, seed_steps));
   }
   return TOTRI_OK;
 }
