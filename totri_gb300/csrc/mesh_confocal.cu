@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
 }
 
 // One CTA per (block of 32 wall points in Morton order, run of `chunks`
-// 32-face chunks): for each chunk, each warp takes one face at a time and its
-// 32 lanes cast the rays from the 32 points, which lie on a compact patch of
+// 32-face chunks): each warp takes one face of the run at a time and its 32
+// lanes cast the rays from the 32 points, which lie on a compact patch of
 // the wall and end on the same centroid, so the lanes walk nearly the same BVH
 // nodes (lockstep model on the 20,480-face sphere: 12% fewer warp iterations
 // and 8.3 -> 5.7 distinct nodes per iteration against point-major warps;
@@ -107,6 +107,7 @@ __global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f 
                                                                int seed_mode, int seed_steps) {
   __shared__ uint32_t bits[kMaxPatchChunks][32];  // [chunk][face j]: visible from point lane
   __shared__ int seeds[32];
+  __shared__ int next_face;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int b = blockIdx.z;
   const int ch0 = blockIdx.y * chunks;
@@ -119,28 +120,35 @@ __global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f 
   volatile int* vseeds = seeds;
   volatile int* gseeds = reinterpret_cast<int*>(sc.pscratch) + (size_t)b * P;
   if (threadIdx.x < 32) seeds[lane] = okp ? gseeds[i] : -1;
+  if (threadIdx.x == 0) next_face = 0;
   __syncthreads();
   const int nc = min(chunks, sc.nch - ch0);
-  for (int c = 0; c < nc; ++c) {
-    for (int j = warp; j < 32; j += 8) {
-      const int k = (ch0 + c) * 32 + j;
-      bool vis = false;
-      if (k < n) {  // warp-uniform
-        const Target tg = load_target(sc, b, k);
-        if (kWalk == 1) {
-          vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
-        } else if (kWalk == 2) {
-          vis = okp && target_visible_pp4(sc, b, n, tg, o, sc.status);
-        } else if (okp) {
-          const int s0 = vseeds[lane];
-          int seed = s0;
-          vis = target_visible_pp(sc, b, n, tg, o, sc.status, seed, seed_mode, seed_steps);
-          if (seed != s0) vseeds[lane] = seed;
-        }
+  // Faces are handed out one at a time from a shared counter, in Morton
+  // order: a hidden face settled by a short surface walk costs a fraction of a
+  // visible one, so fixed shares would leave warps idle at the final barrier.
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(&next_face, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= nc * 32) break;
+    const int c = t >> 5, j = t & 31;
+    const int k = (ch0 + c) * 32 + j;
+    bool vis = false;
+    if (k < n) {  // warp-uniform
+      const Target tg = load_target(sc, b, k);
+      if (kWalk == 1) {
+        vis = packet_visible(sc, b, n, okp, tg, o, sc.status);
+      } else if (kWalk == 2) {
+        vis = okp && target_visible_pp4(sc, b, n, tg, o, sc.status);
+      } else if (okp) {
+        const int s0 = vseeds[lane];
+        int seed = s0;
+        vis = target_visible_pp(sc, b, n, tg, o, sc.status, seed, seed_mode, seed_steps);
+        if (seed != s0) vseeds[lane] = seed;
       }
-      const uint32_t w = __ballot_sync(0xffffffffu, vis);
-      if (lane == 0) bits[c][j] = w;
     }
+    const uint32_t w = __ballot_sync(0xffffffffu, vis);
+    if (lane == 0) bits[c][j] = w;
   }
   __syncthreads();
   if (threadIdx.x < 32 && okp && kWalk == 0) gseeds[i] = seeds[lane];
@@ -514,12 +522,12 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
     if (P >= (1 << 30) / 4) return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points");
     const int st = launch_point_order(sc, pts, P, stream);
     if (st != TOTRI_OK) return st;
-    // Chunks per CTA: 2 while the grid keeps 8 CTAs per SM (10.2 ms against
-    // 11.1 ms for 1 and 10.6 ms for 4 on the 20,480-face workload).
+    // Chunks per CTA: up to 8 while the grid keeps 8 CTAs per SM (20,480-face
+    // workload: 9.15 ms at 8, 9.3 at 4, 9.6 at 2, 10.4 at 1, 10.5 at 16).
     int chunks = tune::get("mesh.visibility.chunks");
     if (chunks <= 0) {
       const int64_t ctas = (int64_t)ceil_div(P, 32) * sc.nch * sc.B;
-      chunks = (int)std::max<int64_t>(1, std::min<int64_t>(2, ctas / (8 * tune::sm_count())));
+      chunks = (int)std::max<int64_t>(1, std::min<int64_t>(8, ctas / (8 * tune::sm_count())));
     }
     if (chunks > kMaxPatchChunks)
       return fail(TOTRI_ERR_INVALID_ARGUMENT, "at most 16 face chunks per visibility block");
