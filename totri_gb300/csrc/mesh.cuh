@@ -203,40 +203,6 @@ __device__ __forceinline__ bool tri_hit(float4 t0, float4 t1, float4 t2, float4 
   return true;
 }
 
-// tri_hit that also returns the barycentric coordinates (u, v) of the ray's
-// crossing with the face's plane, computed where tri_hit stops early as well.
-// The decision and t are tri_hit's: the same operations in the same order.
-__device__ __forceinline__ bool tri_hit_uv(float4 t0, float4 t1, float4 t2, float4 t3, fv3 o,
-                                           fv3 d, float tmax, float& tout, float& uo,
-                                           float& vo) {
-  const fv3 v0 = mkv(t0.x, t0.y, t0.z);
-  const fv3 e1 = mkv(t0.w, t1.x, t1.y);
-  const fv3 e2 = mkv(t1.z, t1.w, t2.x);
-  const fv3 p = xcross(d, e2);
-  const float det = xdot(e1, p);
-  uo = 0.f;
-  vo = 0.f;
-  if (det == 0.f) return false;
-  const float inv = xrcp(det);
-  const fv3 tv = xsub3(o, v0);
-  const float u = xmul(xdot(tv, p), inv);
-  const fv3 q = xcross(tv, e1);
-  const float v = xmul(xdot(d, q), inv);
-  uo = u;
-  vo = v;
-  if (!(u >= 0.f && u <= 1.f)) return false;
-  if (!(v >= 0.f && xadd(u, v) <= 1.f)) return false;
-  const float t = xmul(xdot(e2, q), inv);
-  if (!(t >= 0.f && t <= tmax)) return false;
-  const float px = xfma(t, d.x, o.x);
-  const float py = xfma(t, d.y, o.y);
-  const float pz = xfma(t, d.z, o.z);
-  if (!(px >= t2.y && px <= t3.x && py >= t2.z && py <= t3.y && pz >= t2.w && pz <= t3.z))
-    return false;
-  tout = t;
-  return true;
-}
-
 // Slab test of a BVH box against the ray segment (-inf, limit]. Boxes carry a
 // margin of at least delta beyond every accepted hit point, which dominates
 // the rounding of this test, so a box holding a hit is never rejected. The
@@ -367,25 +333,32 @@ enum SeedMode { kSeedBack = 0, kSeedOff = 1, kSeedAll = 2, kSeedFront = 3 };
 
 // Surface walk: a search for an occluder of the ray from o to target k that
 // starts at face g (the occluder found for a neighbouring query) and moves
-// across the mesh's edges. Each face is tested exactly as the BVH walk tests a
-// leaf; a face that does not occlude hands over to its neighbour beyond the
-// edge that the ray's crossing with its plane lies outside of (the most
-// negative barycentric coordinate). The walk stops at the target, at a mesh
-// boundary, where the crossing lies inside the face, or after `steps` faces.
-// It returns an occluder's Morton position or -1; it can only prove "not
-// visible", so a wrong turn costs time, never a mask bit.
+// across the mesh's edges. The ray's crossing with the current face's plane
+// is located from barycentric coordinates in fast arithmetic (fused
+// multiply-adds, approximate reciprocal); where they put it inside the face,
+// up to a slack, the face gets the exact leaf test of the BVH walk, and an
+// occluder found so ends the walk. Otherwise the walk crosses to the
+// neighbour beyond the edge with the most negative coordinate. It stops at the
+// target, at a mesh boundary, at a face whose plane the ray crosses inside the
+// face without being occluded by it, or after `steps` faces. It returns an
+// occluder's Morton position or -1: only the exact test can end it in "not
+// visible", so the fast coordinates and any wrong turn cost time, never a
+// mask bit.
 __device__ __forceinline__ int surface_walk(const Scene& sc, int b, int n, int k, int f, int g,
                                             fv3 o, fv3 dir, float tmax, float tf, int steps) {
   const float4* tri = sc.tri + (size_t)b * sc.F * 4;
   const int4* adj = sc.adj + (size_t)b * sc.F;
+  constexpr float kSlack = 1e-4f;
   for (int st = 0; st < steps; ++st) {
     if (g == k || (unsigned)g >= (unsigned)n) return -1;
     const float4* q = tri + (size_t)g * 4;
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
-    float tq, u, v;
-    if (tri_hit_uv(q0, q1, q2, q3, o, dir, tmax, tq, u, v) &&
-        (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
-      return g;
+    const fv3 e1 = mkv(q0.w, q1.x, q1.y), e2 = mkv(q1.z, q1.w, q2.x);
+    const fv3 pv = cross(dir, e2);
+    const float inv = __fdividef(1.f, dot(e1, pv));
+    const fv3 tv = o - mkv(q0.x, q0.y, q0.z);
+    const float u = dot(tv, pv) * inv;
+    const float v = dot(dir, cross(tv, e1)) * inv;
     const float w0 = 1.f - u - v;
     int e;
     float wm;
@@ -399,7 +372,15 @@ __device__ __forceinline__ int surface_walk(const Scene& sc, int b, int n, int k
       e = 2;
       wm = v;
     }
-    if (!(wm < 0.f)) return -1;
+    if (wm >= -kSlack) {  // the crossing is inside the face, or close to it
+      float tq;
+      if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
+          (tq < tf || (tq == tf && __float_as_int(q3.w) < f)))
+        return g;
+      if (!(wm < 0.f)) return -1;
+    } else if (!(wm < 0.f)) {
+      return -1;  // NaN coordinates: a degenerate face
+    }
     const int4 a = __ldg(adj + g);
     g = e == 0 ? a.x : (e == 1 ? a.y : a.z);
     if (g < 0) return -1;
