@@ -210,7 +210,8 @@ def _timed(fn, flush, reps, warmup=3):
 def secondary_metrics(device, flush, reps=5):
     """The other throughputs named by the headline metric, on the 128^3 workloads:
     Velten backprojection (128^3 voxels x 128x128 scan points x 1024 bins),
-    volume render + exact adjoint, and RBF splat + gradient (4096 Gaussians)."""
+    volume render + exact adjoint, RBF splat + gradient (4096 Gaussians) and
+    marching cubes + gradient on that RBF volume."""
     from totri_gb300 import scenes
     from totri_gb300.totri_cpp import reconstruct as K
     from totri_gb300.totri_cpp import render as R
@@ -242,8 +243,27 @@ def secondary_metrics(device, flush, reps=5):
     vg = torch.randn_like(rvol)
     ms_rg = _timed(lambda: U.rbf2volume_gaussian_grad(rbf, rvol, vg, rgrad, vd.start, vd.end),
                    flush, reps)
+    from totri_gb300.util.marching_cubes import marching_cubes, marching_cubes_grad
+    U.rbf2volume_gaussian_forward(rbf, rvol, vd.start, vd.end)
+    mc_out = {}
+
+    def mc_forward():
+        mc_out["r"] = marching_cubes(rvol, 0.5, vd.start, vd.end)
+    ms_mc = _timed(mc_forward, flush, reps)
+    verts, edges, tri = mc_out["r"]
+    mgrad = torch.randn_like(verts)
+    ms_mcg = _timed(lambda: marching_cubes_grad(rvol, 0.5, vd.start, vd.end, edges, mgrad),
+                    flush, reps)
+    cells = int(np.prod([r - 1 for r in vd.resolution]))
     pairs = nvox * S
     return {
+        "marching cubes cells/s": {"value": cells / (ms_mc / 1e3), "ms": ms_mc,
+                                   "triangles": int(tri[0]),
+                                   "workload": "RBF volume of 4096 Gaussians, 128^3, iso 0.5, "
+                                               "1 attribute; count + emit with the host "
+                                               "read of the triangle count"},
+        "marching cubes grad vertices/s": {"value": verts.shape[1] / (ms_mcg / 1e3),
+                                           "ms": ms_mcg},
         "backproj voxel·scanpt/s": {"value": pairs / (ms_bp / 1e3), "ms": ms_bp,
                                     "workload": "Velten confocal, 128^3 voxels x 16384 scan "
                                                 "points x 1024 bins"},

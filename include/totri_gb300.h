@@ -386,6 +386,45 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* rbf, const totri_array_t
                                    const float volume_start[3], const float volume_end[3],
                                    void* stream);
 
+/* ----------------------------------------------------------------------- */
+/* util: differentiable marching cubes                                      */
+
+/* Replaces tomcubes.MarchingCubesFunction (an un-vendored submodule of the
+ * reference, .gitmodules:4-6; called at totri/fitting/rbf.py:88-98 as
+ * apply(volume [B,1+A,D,H,W], iso, volume_def.start, volume_def.end) and
+ * rendered as consecutive vertex triples, rbf.py:719). Three calls share one
+ * workspace of totri_marching_cubes_workspace(B, D, H, W) bytes:
+ *   _count: classifies the cells of channel 0 against iso (a grid point is
+ *           inside when its value is above iso) and writes the triangles of
+ *           every batch item to `triangles` [B] int64 (device memory);
+ *   _emit:  writes the triangle soup verts [B,N,3+A] (x, y, z, then the
+ *           attribute channels 1.. interpolated along the same edges) and
+ *           edges [B,N] int64 (12 x cell + edge, the record the gradient
+ *           needs) for N >= 3 x max(triangles); rows past an item's vertices
+ *           are left as the caller filled them (zeros / -1);
+ *   _grad:  accumulates d loss / d volume into volume_grad [B,1+A,D,H,W]
+ *           from verts_grad [B,N,3+A] (rows whose edge record is < 0 are
+ *           skipped), with the case table held constant.
+ * Grid point (x, y, z) sits at start + ((end - start) i) / (n - 1) per axis,
+ * as in totri_rbf2volume_gaussian_forward. */
+size_t totri_marching_cubes_workspace(int64_t batch, int64_t depth, int64_t height,
+                                      int64_t width);
+int totri_marching_cubes_count(const totri_array_t* volume, float iso,
+                               const totri_array_t* triangles, void* workspace,
+                               size_t workspace_bytes, void* stream);
+int totri_marching_cubes_emit(const totri_array_t* volume, float iso,
+                              const float volume_start[3], const float volume_end[3],
+                              const totri_array_t* verts, const totri_array_t* edges,
+                              void* workspace, size_t workspace_bytes, void* stream);
+int totri_marching_cubes_grad(const totri_array_t* volume, float iso,
+                              const float volume_start[3], const float volume_end[3],
+                              const totri_array_t* edges, const totri_array_t* verts_grad,
+                              const totri_array_t* volume_grad, void* stream);
+/* The case table (host memory, no GPU needed): ntri[256] triangles per case
+ * (bit i of the case = corner (i & 1, i >> 1 & 1, i >> 2) inside) and
+ * edges[256 * 15] edge ids (4 x axis + the other two corner bits), -1 padded. */
+int totri_marching_cubes_table(uint8_t* ntri, int8_t* edges);
+
 #ifdef __cplusplus
 }
 #endif

@@ -406,3 +406,10 @@ def rbf2volume_grad(rbf, volume, volume_grad, start, end):
                                  _ptr(v, _f64p), _ptr(g, _f64p), _ptr(a, _f32p), _ptr(e, _f32p),
                                  _ptr(out, _f64p))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Marching cubes (numpy restatement with its own case-table derivation).
+
+from .isosurface import case_table as marching_cubes_table  # noqa: E402
+from .isosurface import marching_cubes, marching_cubes_grad  # noqa: E402,F401

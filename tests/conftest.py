@@ -28,3 +28,12 @@ def oracle_lib():
     import oracle
     oracle.lib()
     return oracle
+
+
+@pytest.fixture(scope="session")
+def cuda_free_lib():
+    """Builds (incrementally) and loads libtotri_gb300.so for its host-only
+    entry points and argument checks (no GPU needed)."""
+    from totri_gb300 import build, _lib
+    build.build()
+    return _lib.load()

@@ -89,6 +89,12 @@ _SIGNATURES = {
                                                                        _vp],
     "totri_rbf2volume_gaussian_forward": [_ArrP] * 2 + [_F3, _F3, _vp],
     "totri_rbf2volume_gaussian_grad": [_ArrP] * 4 + [_F3, _F3, _vp],
+    "totri_marching_cubes_workspace": [_i64, _i64, _i64, _i64],
+    "totri_marching_cubes_count": [_ArrP, _flt, _ArrP, _vp, _sz, _vp],
+    "totri_marching_cubes_emit": [_ArrP, _flt, _F3, _F3, _ArrP, _ArrP, _vp, _sz, _vp],
+    "totri_marching_cubes_grad": [_ArrP, _flt, _F3, _F3, _ArrP, _ArrP, _ArrP, _vp],
+    "totri_marching_cubes_table": [ctypes.POINTER(ctypes.c_uint8),
+                                   ctypes.POINTER(ctypes.c_int8)],
 }
 _RESTYPES = {
     "totri_version": ctypes.c_char_p,
@@ -96,6 +102,7 @@ _RESTYPES = {
     "totri_mesh_workspace": ctypes.c_size_t,
     "totri_mesh_mask_bytes": ctypes.c_size_t,
     "totri_volume_workspace": ctypes.c_size_t,
+    "totri_marching_cubes_workspace": ctypes.c_size_t,
     "totri_profile_reset": None,
 }
 
