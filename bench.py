@@ -207,6 +207,31 @@ def _timed(fn, flush, reps, warmup=3):
     return total / reps
 
 
+def pose_fit_rate(device, iterations=50):
+    """(iterations, device-timed ms) of one rigid pose fit on the plain
+    confocal workload (320 faces, 32x32 scan, 512 bins), target offset by
+    (3, -2, 4) cm."""
+    from totri_gb300 import scenes
+    from totri_gb300.fitting import PoseFitting
+    from totri_gb300.render import MeshRenderConfocal
+    s = scenes.confocal_small(seed=2)
+    v, f, sp = (s[k][0].to(device) for k in ("verts", "faces", "scan_points"))
+    bd = s["bin_def"]
+    with torch.no_grad():
+        target = MeshRenderConfocal.apply(
+            (v + torch.tensor((0.03, -0.02, 0.04), device=device))[None], f[None], sp[None],
+            bd)[0]
+    PoseFitting(bd).fit(target, sp, [v], [f], num_iter=3, stop_loss=None)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    PoseFitting(bd).fit(target, sp, [v], [f], num_iter=iterations, stop_loss=None)
+    e1.record(stream)
+    e1.synchronize()
+    return iterations, e0.elapsed_time(e1)
+
+
 def secondary_metrics(device, flush, reps=5):
     """The other throughputs named by the headline metric, on the 128^3 workloads:
     Velten backprojection (128^3 voxels x 128x128 scan points x 1024 bins),
@@ -256,7 +281,13 @@ def secondary_metrics(device, flush, reps=5):
                     flush, reps)
     cells = int(np.prod([r - 1 for r in vd.resolution]))
     pairs = nvox * S
+    fit_iter, ms_fit = pose_fit_rate(device)
     return {
+        "pose fit iterations/s": {"value": fit_iter / (ms_fit / 1e3), "ms": ms_fit,
+                                  "workload": "PoseFitting (translation + quaternion, Adam) "
+                                              "of a 320-face mesh to a 32x32 x 512-bin "
+                                              "transient, %d iterations, no early stop"
+                                              % fit_iter},
         "marching cubes cells/s": {"value": cells / (ms_mc / 1e3), "ms": ms_mc,
                                    "triangles": int(tri[0]),
                                    "workload": "RBF volume of 4096 Gaussians, 128^3, iso 0.5, "

@@ -23,7 +23,12 @@ Kinds (``Request.kind``):
                     ``target`` and its gradients: (loss, verts_grad [V, 3],
                     colors_grad [V, 1]);
   * "backproject" — Velten confocal backprojection of measurement ``target``
-                    into ``volume`` (a VolumeDef): volume [D, H, W].
+                    into ``volume`` (a VolumeDef): volume [D, H, W];
+  * "fit_pose"    — ``iterations`` steps of the rigid pose fit of mesh ``mesh``
+                    to measurement ``target`` (``fitting.PoseFitting``, no
+                    early stop): (translation [3], quaternion [4], losses
+                    [iterations]). The pose changes the geometry every step,
+                    so each step rebuilds the BVH and masks in its own scratch.
 """
 import collections
 import concurrent.futures
@@ -48,6 +53,7 @@ class Request:
     bins: typing.Optional[BinDef] = None
     target: typing.Optional[str] = None
     volume: typing.Optional[VolumeDef] = None
+    iterations: int = 0
     # filled in by the server
     id: int = -1
     arrival: float = 0.0
@@ -205,24 +211,26 @@ class Server:
     def _validate(self, r):
         if r.grid not in self.grids:
             raise KeyError("unknown grid %r" % r.grid)
-        if r.kind in ("render", "grad"):
+        if r.kind in ("render", "grad", "fit_pose"):
             if r.mesh not in self.meshes:
                 raise KeyError("unknown mesh %r" % r.mesh)
             if r.bins is None:
-                raise ValueError("render/grad requests need bins")
-        if r.kind in ("grad", "backproject"):
+                raise ValueError("render/grad/fit_pose requests need bins")
+        if r.kind == "fit_pose" and r.iterations < 1:
+            raise ValueError("fit_pose requests need iterations >= 1")
+        if r.kind in ("grad", "backproject", "fit_pose"):
             if r.target not in self.measurements:
                 raise KeyError("unknown measurement %r" % r.target)
             tr, grid, bins = self.measurements[r.target]
             if grid != r.grid:
                 raise ValueError("measurement %r is on grid %r" % (r.target, grid))
-            if r.kind == "grad" and (bins.num, bins.width, bins.offset) != (
+            if r.kind in ("grad", "fit_pose") and (bins.num, bins.width, bins.offset) != (
                     r.bins.num, r.bins.width, r.bins.offset):
                 raise ValueError("measurement %r is binned differently from the request"
                                  % r.target)
         if r.kind == "backproject" and r.volume is None:
             raise ValueError("backproject requests need a VolumeDef")
-        if r.kind not in ("render", "grad", "backproject"):
+        if r.kind not in ("render", "grad", "backproject", "fit_pose"):
             raise ValueError("unknown request kind %r" % r.kind)
 
     def _mask_bytes(self, r):
@@ -236,6 +244,9 @@ class Server:
         if r.kind == "backproject":
             return 4 * int(torch.tensor(r.volume.resolution).prod())
         m = self.meshes[r.mesh]
+        if r.kind == "fit_pose":  # per step: scratch with masks, two transients, gradients
+            ws = int(self.lib.totri_mesh_workspace(1, m.verts.shape[1], m.F, S))
+            return ws + 3 * 4 * r.bins.num * S + 8 * 4 * m.verts.shape[1]
         need = 4 * r.bins.num * S
         if r.kind == "grad":
             need = 2 * need + 4 * 4 * m.verts.shape[1]
@@ -253,6 +264,8 @@ class Server:
         sp = self.grids[r.grid]
         S = sp.shape[1]
         key = None
+        if r.kind == "fit_pose":
+            return self._fit_pose(r)
         if r.kind in ("render", "grad"):
             m = self.meshes[r.mesh]
             key = (r.mesh, r.grid)
@@ -309,6 +322,25 @@ class Server:
         host = torch.empty(vol.shape[1:], dtype=torch.float32, pin_memory=True)
         host.copy_(vol[0], non_blocking=True)
         return host
+
+    def _fit_pose(self, r):
+        """Enqueues the pose fit on the current stream; no host synchronisation."""
+        from .fitting import PoseFitting
+        m = self.meshes[r.mesh]
+        target = self.measurements[r.target][0]
+        target.record_stream(torch.cuda.current_stream(self.device))
+        fitting = PoseFitting(r.bins)
+        (t,), (q,) = fitting.fit(target[0], self.grids[r.grid][0], [m.verts[0]],
+                                 [m.faces[0]], num_iter=r.iterations, stop_loss=None,
+                                 colors_list=[m.colors[0]])
+        losses = torch.stack(fitting.losses)
+        out = (torch.empty(3, dtype=torch.float32, pin_memory=True),
+               torch.empty(4, dtype=torch.float32, pin_memory=True),
+               torch.empty(r.iterations, dtype=torch.float32, pin_memory=True))
+        out[0].copy_(t.translation.detach()[0], non_blocking=True)
+        out[1].copy_(q.quaternion.detach()[0], non_blocking=True)
+        out[2].copy_(losses, non_blocking=True)
+        return out
 
     def _admit_one(self):
         """Admits the first of the next `lookahead` queued requests that fits."""
