@@ -43,3 +43,57 @@ def test_merge_meshes_offsets_faces():
     v, f = merge_meshes([v0, v1], [f0, f1])
     assert v.shape == (9, 3)
     assert f.tolist() == [[0, 1, 2], [4, 5, 6], [6, 7, 8]]
+
+
+def test_depth_map_geometry_and_clamps():
+    from totri_gb300.fitting import DepthMap
+    from totri_gb300.types import VolumeDef
+    dm = DepthMap(VolumeDef((-0.5, -0.5, 0.5), (0.5, 0.5, 1.5), (8, 4, 5)), device="cpu")
+    v = dm.verts()
+    assert v.shape == (20, 3) and dm.faces.shape == (24, 3)
+    assert v[:5, 0].tolist() == [-0.5, -0.25, 0.0, 0.25, 0.5]
+    assert abs(float(v[5, 1]) - (-0.5 + 1 / 3)) < 1e-6
+    assert torch.all(v[:, 2] == 1.0)
+    assert dm.faces[:2].tolist() == [[0, 6, 1], [0, 5, 6]]
+    with torch.no_grad():
+        dm.depth[:] = 2.0
+        dm.color[:] = 4.0
+    intensity = torch.ones(1)
+    dm.clamp_params(intensity)
+    assert dm.depth[1, 1] == 1.0 and dm.depth[0, 0] == 0.5
+    assert dm.color[1, 1] == 1.0 and float(intensity) == 4.0
+
+
+def test_tv_loss_and_blur():
+    from totri_gb300.fitting import tv_loss
+    from totri_gb300.fitting.depth_map import gaussian_blur
+    assert abs(float(tv_loss(torch.ones(6, 7)))) < 1e-7
+    t = torch.zeros(4, 4)
+    t[1, 1] = 1.0
+    # nonzero differences: dx at (1,0) and (1,1), dy at (0,1) and (1,1)
+    eps = 1e-3
+    expect = (2 * (1 + eps) ** 0.5 + (2 + eps) ** 0.5 - 3 * eps ** 0.5) / 16
+    assert abs(float(tv_loss(t)) - expect) < 1e-6
+    img = torch.rand(2, 11, 13, dtype=torch.float64)
+    out = gaussian_blur(img, 9)
+    assert out.shape == img.shape
+    assert torch.allclose(gaussian_blur(torch.ones(1, 9, 9), 9), torch.ones(1, 9, 9))
+    assert abs(float(out.mean() - img.mean())) < 0.05
+
+
+def test_optimizer_schedule():
+    from totri_gb300.util.optim import (LinearInterpolator, MultiplicativeInterpolator,
+                                        TotriOptimizer)
+    p = torch.zeros(2, requires_grad=True)
+    opt = TotriOptimizer([p], 1.0, warmup=3)
+    assert opt.lr == (1 / 4) ** 2
+    rates = []
+    for _ in range(4):
+        p.sum().backward()
+        opt.step()
+        rates.append(opt.optim.param_groups[0]["lr"])
+    assert rates == [(2 / 4) ** 2, (3 / 4) ** 2, 1.0, 1.0]
+    lin = LinearInterpolator(1.0, 3.0, 5)
+    assert [lin(i) for i in (0, 2, 4, 9)] == [1.0, 2.0, 3.0, 3.0]
+    mul = MultiplicativeInterpolator(1.0, 0.0, 0.5)
+    assert [mul(0), mul(0)] == [0.5, 0.25]

@@ -106,5 +106,55 @@ def test_fit_request_alone_and_in_the_mix(cuda_lib):
     assert torch.allclose(alone[0], mixed[0], atol=1e-4)  # translation (m)
     qa, qb = alone[1] / alone[1].norm(), mixed[1] / mixed[1].norm()
     assert torch.allclose(qa, qb, atol=1e-4)
-    assert torch.allclose(alone[2], mixed[2], rtol=1e-3, atol=1e-6)
+    # losses along the way: FP32 gradients summed by atomics in either order
+    assert float((alone[2] - mixed[2]).abs().max()) <= 1e-3 * float(alone[2].max())
     assert float(alone[2][-1]) < float(alone[2][0])
+
+
+def _bump_target(res=16, laser=False):
+    from totri_gb300.fitting import DepthMap
+    from totri_gb300.types import VolumeDef
+    vd = VolumeDef((-0.4, -0.4, 0.6), (0.4, 0.4, 1.4), (1, res, res))
+    truth = DepthMap(VolumeDef(vd.start, vd.end, vd.resolution))
+    y, x = torch.meshgrid(torch.linspace(-1, 1, res), torch.linspace(-1, 1, res), indexing="ij")
+    with torch.no_grad():
+        truth.depth[:] = (0.5 + 0.3 * torch.exp(-(x * x + y * y) / 0.3)).cuda()
+        truth.clamp_params(None)
+    sp = scenes.wall_grid(24)[0].cuda()
+    lp = scenes.wall_grid(4)[0].cuda() if laser else None
+    bd = BinDef(0.01, 0.0, 400)
+    with torch.no_grad():
+        if laser:
+            from totri_gb300.render import MeshRenderExhaustive
+            target = MeshRenderExhaustive.apply(truth.verts()[None], truth.faces[None], sp[None],
+                                                lp[None], bd, truth.color.view(1, -1, 1))[0]
+        else:
+            target = MeshRenderConfocal.apply(truth.verts()[None], truth.faces[None], sp[None],
+                                              bd, truth.color.view(1, -1, 1))[0]
+    return vd, truth, sp, lp, bd, target
+
+
+def test_depth_map_fitting_reduces_loss_and_depth_error(cuda_lib):
+    from totri_gb300.fitting import DepthMap, DepthMapFitting
+    from totri_gb300.types import VolumeDef
+    vd, truth, sp, _, bd, target = _bump_target()
+    dm = DepthMap(VolumeDef(vd.start, vd.end, vd.resolution))
+    err0 = float((dm.depth - truth.depth).abs().mean())
+    fit = DepthMapFitting(bd)
+    fit.fit(dm, target, sp, num_iter=150, lambda_depth=0.02, lambda_color=0.01)
+    assert float(fit.losses[-1]) < 0.2 * float(fit.losses[0])
+    assert float((dm.depth - truth.depth).abs().mean()) < 0.75 * err0
+
+
+def test_depth_map_fitting_exhaustive_subsets_and_subdivision(cuda_lib):
+    """The exhaustive render, scan-point subsets and a grid refinement in one
+    short run: the loss stays finite and the grid doubles."""
+    from totri_gb300.fitting import DepthMap, DepthMapFitting
+    from totri_gb300.types import VolumeDef
+    vd, _, sp, lp, bd, target = _bump_target(res=8, laser=True)
+    dm = DepthMap(VolumeDef(vd.start, vd.end, vd.resolution))
+    fit = DepthMapFitting(bd)
+    fit.fit(dm, target, sp, laser_points=lp, scan_point_limit=200, num_iter=6,
+            subdivide_at=[3])
+    assert dm.depth.shape == (16, 16) and dm.faces.shape[0] == 2 * 15 * 15
+    assert all(torch.isfinite(l) for l in fit.losses)

@@ -1,4 +1,6 @@
 """Fitting loops over the differentiable renderer (reference totri/fitting)."""
+from .depth_map import DepthMap, DepthMapFitting, tv_loss
 from .pose import PoseFitting, Rotation, Translation, apply_transform, quaternion_apply
 
-__all__ = ["PoseFitting", "Rotation", "Translation", "apply_transform", "quaternion_apply"]
+__all__ = ["DepthMap", "DepthMapFitting", "tv_loss", "PoseFitting", "Rotation", "Translation",
+           "apply_transform", "quaternion_apply"]
