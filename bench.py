@@ -235,8 +235,9 @@ def pose_fit_rate(device, iterations=50):
 def secondary_metrics(device, flush, reps=5):
     """The other throughputs named by the headline metric, on the 128^3 workloads:
     Velten backprojection (128^3 voxels x 128x128 scan points x 1024 bins),
-    volume render + exact adjoint, RBF splat + gradient (4096 Gaussians) and
-    marching cubes + gradient on that RBF volume."""
+    volume render + exact adjoint, RBF splat + gradient (4096 Gaussians),
+    marching cubes + gradient on that RBF volume, a pose fit and f-k
+    migration."""
     from totri_gb300 import scenes
     from totri_gb300.totri_cpp import reconstruct as K
     from totri_gb300.totri_cpp import render as R
@@ -282,7 +283,14 @@ def secondary_metrics(device, flush, reps=5):
     cells = int(np.prod([r - 1 for r in vd.resolution]))
     pairs = nvox * S
     fit_iter, ms_fit = pose_fit_rate(device)
+    from totri_gb300.reconstruct import FkMigration
+    fk_in = torch.rand((1, 512, 64, 64), device=device) ** 4
+    fk = FkMigration(512 * 0.005, 2.0, 2.0)
+    ms_fk = _timed(lambda: fk(fk_in), flush, reps)
     return {
+        "fk migration voxels/s": {"value": 512 * 64 * 64 / (ms_fk / 1e3), "ms": ms_fk,
+                                  "workload": "512 bins x 64 x 64 scan points (2 x 512 x 64 x "
+                                              "64 complex FFTs, cuFFT through torch.fft)"},
         "pose fit iterations/s": {"value": fit_iter / (ms_fit / 1e3), "ms": ms_fit,
                                   "workload": "PoseFitting (translation + quaternion, Adam) "
                                               "of a 320-face mesh to a 32x32 x 512-bin "

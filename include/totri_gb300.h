@@ -387,6 +387,27 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* rbf, const totri_array_t
                                    void* stream);
 
 /* ----------------------------------------------------------------------- */
+/* reconstruct: f-k migration                                               */
+
+/* The three kernels of totri.reconstruct.FkMigration (reference
+ * totri/reconstruct/fk_migration.py:88-120, plain PyTorch there); the caller
+ * runs the forward and inverse 3-D FFTs between them. Complex arrays are
+ * float32 with a trailing dimension of 2 (re, im).
+ *   _prepare: transient [N,D,H,W] -> out [N,2D,H,W,2]: sqrt(t) x
+ *             linspace(0,1,D)[d] for d < D, zero for the padding bins;
+ *   _stolt:   Stolt resampling (StoltInterpolation, fk_migration.py:5-86) of
+ *             fourier [M,2D,H,W,2] into out (not in place); input_centred 0
+ *             reads an un-centred FFT as if fftshift had been applied,
+ *             output_centred 0 writes the result ifftshift-ed;
+ *   _finish:  volume [N,2D,H,W,2] -> out [N,D,H,W] = |volume| of the first D
+ *             bins. */
+int totri_fk_prepare(const totri_array_t* transient, const totri_array_t* out, void* stream);
+int totri_fk_stolt(const totri_array_t* fourier, const totri_array_t* out, float depth,
+                   float height, float width, int input_centred, int output_centred,
+                   void* stream);
+int totri_fk_finish(const totri_array_t* volume, const totri_array_t* out, void* stream);
+
+/* ----------------------------------------------------------------------- */
 /* util: differentiable marching cubes                                      */
 
 /* Replaces tomcubes.MarchingCubesFunction (an un-vendored submodule of the

@@ -413,3 +413,9 @@ def rbf2volume_grad(rbf, volume, volume_grad, start, end):
 
 from .isosurface import case_table as marching_cubes_table  # noqa: E402
 from .isosurface import marching_cubes, marching_cubes_grad  # noqa: E402,F401
+
+
+# ---------------------------------------------------------------------------
+# f-k migration (numpy restatement).
+
+from .fk import fk_migration, stolt  # noqa: E402,F401

@@ -89,6 +89,9 @@ _SIGNATURES = {
                                                                        _vp],
     "totri_rbf2volume_gaussian_forward": [_ArrP] * 2 + [_F3, _F3, _vp],
     "totri_rbf2volume_gaussian_grad": [_ArrP] * 4 + [_F3, _F3, _vp],
+    "totri_fk_prepare": [_ArrP, _ArrP, _vp],
+    "totri_fk_stolt": [_ArrP, _ArrP, _flt, _flt, _flt, _int, _int, _vp],
+    "totri_fk_finish": [_ArrP, _ArrP, _vp],
     "totri_marching_cubes_workspace": [_i64, _i64, _i64, _i64],
     "totri_marching_cubes_count": [_ArrP, _flt, _ArrP, _vp, _sz, _vp],
     "totri_marching_cubes_emit": [_ArrP, _flt, _F3, _F3, _ArrP, _ArrP, _vp, _sz, _vp],
