@@ -135,22 +135,26 @@ def test_velten_bins_exact(cuda_lib, offset, origin):
 
 def test_velten_tiled_equals_untiled(cuda_lib):
     """The shared-memory tiled Velten kernel sums the same values in the same
-    order as the one-voxel-per-thread kernel: identical volumes, including a
-    grid that is not a multiple of the 8x8x4 voxel block and a scan whose
-    bin windows overflow the staged rows."""
+    order as the one-voxel-per-thread kernel: identical volumes for 1, 2 and
+    4 voxels per thread, including grids that are not a multiple of the voxel
+    block and a scan whose bin windows overflow the staged rows."""
     from totri_gb300 import autotune
     g = np.random.default_rng(5)
-    for res, S, T, bw in (((37, 29, 50), 300, 900, 0.004), ((16, 16, 16), 1000, 256, 0.05)):
+    for res, S, T, bw in (((37, 29, 50), 300, 900, 0.004), ((16, 16, 16), 1000, 256, 0.05),
+                          ((21, 9, 11), 77, 400, 0.01)):
         tr = torch.from_numpy(g.random((1, T, S), dtype=np.float32)).cuda()
         sp = torch.from_numpy(np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S),
                                         np.zeros(S)], -1).astype(np.float32))[None].cuda()
         out = []
-        for mode in (0, 1):
+        for mode, vz in ((1, 0), (0, 1), (0, 2), (0, 4)):
             autotune.set_tile("backprojection.velten.mode", mode)
+            autotune.set_tile("backprojection.velten.vz", vz)
             v = torch.empty((1,) + res, device="cuda")
             K.backprojection_confocal_velten_forward(tr, sp, torch.empty((1, 0, 3), device="cuda"),
                                                      v, (-0.5, -0.4, 0.5), (0.5, 0.45, 1.5), bw,
                                                      0.01)
             out.append(v)
         autotune.set_tile("backprojection.velten.mode", 0)
-        assert torch.equal(out[0], out[1])
+        autotune.set_tile("backprojection.velten.vz", 0)
+        for o in out[1:]:
+            assert torch.equal(out[0], o)
