@@ -408,6 +408,22 @@ int totri_fk_stolt(const totri_array_t* fourier, const totri_array_t* out, float
 int totri_fk_finish(const totri_array_t* volume, const totri_array_t* out, void* stream);
 
 /* ----------------------------------------------------------------------- */
+/* util: orthographic depth rasteriser                                      */
+
+/* Replaces totri.util.UnitDepthMapRender (totri/util/depthmap.py:6-36, a
+ * pytorch3d orthographic rasteriser): verts [V,3] float32, faces [F,3] int64
+ * -> depth [H,W] float32 (nearest face's z at each pixel centre within
+ * [znear, zfar], -1 where empty) and mask [H,W] int32 (1 where covered).
+ * Column j looks along x = max_x - (j + 1/2) (max_x - min_x) / W, row i along
+ * y = max_y - (i + 1/2) (max_y - min_y) / H, both faces counted. Scratch:
+ * totri_depth_raster_workspace(H, W) bytes. */
+size_t totri_depth_raster_workspace(int64_t height, int64_t width);
+int totri_depth_raster(const totri_array_t* verts, const totri_array_t* faces,
+                       const totri_array_t* depth, const totri_array_t* mask, float min_x,
+                       float max_x, float min_y, float max_y, float znear, float zfar,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* ----------------------------------------------------------------------- */
 /* util: differentiable marching cubes                                      */
 
 /* Replaces tomcubes.MarchingCubesFunction (an un-vendored submodule of the

@@ -419,3 +419,9 @@ from .isosurface import marching_cubes, marching_cubes_grad  # noqa: E402,F401
 # f-k migration (numpy restatement).
 
 from .fk import fk_migration, stolt  # noqa: E402,F401
+
+
+# ---------------------------------------------------------------------------
+# Orthographic depth rasteriser (numpy restatement).
+
+from .raster import depth_raster  # noqa: E402,F401

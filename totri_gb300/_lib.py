@@ -89,6 +89,8 @@ _SIGNATURES = {
                                                                        _vp],
     "totri_rbf2volume_gaussian_forward": [_ArrP] * 2 + [_F3, _F3, _vp],
     "totri_rbf2volume_gaussian_grad": [_ArrP] * 4 + [_F3, _F3, _vp],
+    "totri_depth_raster_workspace": [_i64, _i64],
+    "totri_depth_raster": [_ArrP] * 4 + [_flt] * 6 + [_vp, _sz, _vp],
     "totri_fk_prepare": [_ArrP, _ArrP, _vp],
     "totri_fk_stolt": [_ArrP, _ArrP, _flt, _flt, _flt, _int, _int, _vp],
     "totri_fk_finish": [_ArrP, _ArrP, _vp],
@@ -106,6 +108,7 @@ _RESTYPES = {
     "totri_mesh_mask_bytes": ctypes.c_size_t,
     "totri_volume_workspace": ctypes.c_size_t,
     "totri_marching_cubes_workspace": ctypes.c_size_t,
+    "totri_depth_raster_workspace": ctypes.c_size_t,
     "totri_profile_reset": None,
 }
 
