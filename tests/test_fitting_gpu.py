@@ -158,3 +158,55 @@ def test_depth_map_fitting_exhaustive_subsets_and_subdivision(cuda_lib):
             subdivide_at=[3])
     assert dm.depth.shape == (16, 16) and dm.faces.shape[0] == 2 * 15 * 15
     assert all(torch.isfinite(l) for l in fit.losses)
+
+
+def _rbf_problem():
+    from totri_gb300.fitting import GaussianRbfBase
+    from totri_gb300.types import VolumeDef
+    vd = VolumeDef((-0.5, -0.5, 0.5), (0.5, 0.5, 1.5), (24, 24, 24))
+    truth = GaussianRbfBase(VolumeDef(vd.start, vd.end, vd.resolution))
+    for x, y, z in ((-0.1, 0.05, 0.95), (0.12, -0.08, 1.05), (0.0, 0.15, 1.1)):
+        truth.append(x, y, z)
+    sp = scenes.wall_grid(16)[0].cuda()
+    bd = BinDef(0.01, 0.0, 320)
+    return vd, truth, sp, bd
+
+
+def test_rbf_optimize_reduces_loss(cuda_lib):
+    """The inner loop (Adam through RBF splat -> marching cubes -> render)
+    moves perturbed blobs towards the ones that made the measurement."""
+    from totri_gb300.fitting import RbfFitting, TransientBackgroundEmpty
+    vd, truth, sp, bd = _rbf_problem()
+    fit = RbfFitting(bd, sp)
+    with torch.no_grad():
+        target = fit.base_to_transient(truth, TransientBackgroundEmpty(),
+                                       torch.ones(1, device="cuda"))[1]
+    target = target / target.mean()
+    base = truth.clone()
+    with torch.no_grad():
+        base.params[:, :3] += torch.tensor([[0.04, -0.03, 0.03]], device="cuda")
+    bg = TransientBackgroundEmpty()
+    _, before = fit.loss_all(base, bg, target)
+    losses, after, iters = fit.optimize(base, bg, target, num_iter=150)
+    assert iters > 10
+    assert float(after) < 0.5 * float(before)
+
+
+def test_rbf_fit_moves_add_blobs(cuda_lib):
+    """Three driver moves from no blobs at all: the volume and surface moves
+    add blobs and the loss falls below that of the empty base."""
+    from totri_gb300.fitting import GaussianRbfBase, RbfFitting, TransientBackgroundEmpty
+    from totri_gb300.types import VolumeDef
+    vd, truth, sp, bd = _rbf_problem()
+    fit = RbfFitting(bd, sp)
+    with torch.no_grad():
+        target = fit.base_to_transient(truth, TransientBackgroundEmpty(),
+                                       torch.ones(1, device="cuda"))[1]
+    torch.manual_seed(0)
+    base = GaussianRbfBase(VolumeDef(vd.start, vd.end, vd.resolution))
+    norm = target / target.mean()
+    _, empty_loss = fit.loss_all(base, TransientBackgroundEmpty(), norm)
+    out = fit.fit(base, target, num_iter=2)
+    _, final = fit.loss_all(out, TransientBackgroundEmpty(), norm)
+    assert out.num_rbf() > 0
+    assert float(final) < float(empty_loss)
