@@ -244,8 +244,8 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
   }
 }
 
-// Exact adjoint of the forward: one CTA per voxel column, threads over
-// points, each walking the bins whose samples land in the column. Each warp
+// Exact adjoint of the forward: one CTA per voxel column, a warp per point,
+// walking the bins whose samples land in the column. Each warp
 // accumulates into its own copy of the column in shared memory (eight copies:
 // the 256 threads' atomics no longer pile onto one Z-vector), summed at the end.
 __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp, int N,
@@ -256,9 +256,15 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
   const int xi = c / g.Y, yi = c - xi * g.Y;
   for (int z = threadIdx.x; z < 8 * g.Z; z += blockDim.x) cols[z] = 0.f;
   __syncthreads();
-  float* col = cols + (threadIdx.x >> 5) * g.Z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* col = cols + warp * g.Z;
   const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  // a warp per point, its lanes over the point's bins: every lane has work
+  // until the walk's last 32 bins, the transient row is read 128 bytes at a
+  // time, and neighbouring lanes' samples fall in neighbouring cells (194 ms
+  // with a thread per point; 240 ms with half a warp per point, 148 ms here,
+  // on 128^3 voxels x 16,384 points x 1,024 bins)
+  for (int i = warp; i < N; i += blockDim.x >> 5) {
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
     const float rho2 = (wx - x) * (wx - x) + (wy - y) * (wy - y);
     // bins covering the whole column: interpolation cells 0 .. Z-2
@@ -266,7 +272,7 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
     bin_range(g, rho2, wz, 1, t0, t1);
     bin_range(g, rho2, wz, g.Z - 1, u0, u1);
     const float* row = tr + (size_t)i * g.T;
-    for (int t = t0; t <= u1; ++t) {
+    for (int t = t0 + lane; t <= u1; t += 32) {
       const Sample s = sample_filtered(g, wx, wy, wz, t, x, y);
       if (!s.ok) continue;
       const float v = __ldg(row + t) * s.f2;
