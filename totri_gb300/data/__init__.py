@@ -1,4 +1,6 @@
-"""totri_gb300.data: wall grids and mesh helpers (reference totri/data/util.py)."""
+"""totri_gb300.data: wall grids, mesh helpers (reference totri/data/util.py) and
+the MATLAB-format dataset loaders (veltennc2012.py, otooleconfocal2018.py)."""
+from .mat_datasets import OTooleConfocal2018, VeltenNc2012
 from .util import make_wall_grid, merge_meshes
 
-__all__ = ["make_wall_grid", "merge_meshes"]
+__all__ = ["make_wall_grid", "merge_meshes", "OTooleConfocal2018", "VeltenNc2012"]
