@@ -233,7 +233,7 @@ __device__ __forceinline__ float alpha_confocal(const ConfocalPair& q, fv3 c, fv
   if (!(r.z > 0.f)) return 0.f;
   const float nr = dot(n, r), rr = dot(r, r), nn = dot(n, n);
   const float rr2 = rr * rr;
-  return 100.f * rho * (r.z * r.z) * (nr * nr) / (sqrtf(nn) * (rr2 * rr2));
+  return vdiv(100.f * rho * (r.z * r.z) * (nr * nr), sqrtf(nn) * (rr2 * rr2));
 }
 
 template <int TS>
@@ -371,17 +371,17 @@ __device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c,
   const fv3 n = cross(e1, e2);
   const fv3 r = c - p;
   // d log(alpha) / d v_k = J_n^T (kn n + knr r) + kr r + (knr/3) n + kw n_w
-  const float kn = -1.f / dot(n, n);
-  const float kr = -8.f / (3.f * dot(r, r));
-  const float kw = 2.f / (3.f * r.z);
-  const float knr = 2.f / dot(n, r);
+  const float kn = vdiv(-1.f, dot(n, n));
+  const float kr = vdiv(-8.f, 3.f * dot(r, r));
+  const float kw = vdiv(2.f, 3.f * r.z);
+  const float knr = vdiv(2.f, dot(n, r));
   const fv3 w = kn * n + knr * r;
   const fv3 g1 = cross(e2, w), g2 = cross(w, e1);
   const fv3 common = kr * r + (knr * (1.f / 3.f)) * n + mkv(0.f, 0.f, kw);
   const fv3 da0 = alpha * (common - g1 - g2);
   const fv3 da1 = alpha * (common + g1);
   const fv3 da2 = alpha * (common + g2);
-  const float dadm = alpha / rho;
+  const float dadm = vdiv(alpha, rho);
   if (q.bin[0] == q.bin[2]) {
     const float g = __ldg(tg_col + (size_t)q.bin[0] * S);
     dv[0] = g * da0;
@@ -394,13 +394,13 @@ __device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c,
   tent_grad(tg_col, S, T, q.c, q.bin, tgr);
   // part1 = Ayc * dyc + A0 * dc0 + A1 * dc1 + A2 * dc2 (see TentGrad)
   const float span = q.c[2] - q.c[0];
-  const float kk = -4.f / (bw * span * span);
+  const float kk = vdiv(-4.f, bw * span * span);
   const fv3 r0 = q.v[0] - p, r1 = q.v[1] - p, r2 = q.v[2] - p;
-  const fv3 dc0 = (2.f / (bw * q.d[0])) * r0;
-  const fv3 dc1 = (2.f / (bw * q.d[1])) * r1;
-  const fv3 dc2 = (2.f / (bw * q.d[2])) * r2;
-  const fv3 dyc0 = (kk / -q.d[0]) * r0;
-  const fv3 dyc2 = (kk / q.d[2]) * r2;
+  const fv3 dc0 = vdiv(2.f, bw * q.d[0]) * r0;
+  const fv3 dc1 = vdiv(2.f, bw * q.d[1]) * r1;
+  const fv3 dc2 = vdiv(2.f, bw * q.d[2]) * r2;
+  const fv3 dyc0 = vdiv(kk, -q.d[0]) * r0;
+  const fv3 dyc2 = vdiv(kk, q.d[2]) * r2;
   const fv3 p1_0 = tgr.ayc * dyc0 + tgr.a0 * dc0;
   const fv3 p1_1 = tgr.a1 * dc1;
   const fv3 p1_2 = tgr.ayc * dyc2 + tgr.a2 * dc2;

@@ -104,8 +104,8 @@ __device__ __forceinline__ float alpha_exhaustive(const ExhPair& q, fv3 c, fv3 s
   const fv3 rs = c - sp, rl = c - lp;
   if (!(rs.z > 0.f) || !(rl.z > 0.f)) return 0.f;
   const float rss = dot(rs, rs), rll = dot(rl, rl);
-  return 100.f * rho * rs.z * rl.z * fabsf(dot(n, rs)) * fabsf(dot(n, rl)) /
-         (sqrtf(dot(n, n)) * (rss * rss) * (rll * rll));
+  return vdiv(100.f * rho * rs.z * rl.z * fabsf(dot(n, rs)) * fabsf(dot(n, rl)),
+              sqrtf(dot(n, n)) * (rss * rss) * (rll * rll));
 }
 
 __device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int l, fv3 sp,
@@ -255,17 +255,17 @@ __device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3
   const fv3 e1 = q.v[1] - q.v[0], e2 = q.v[2] - q.v[0];
   const fv3 n = cross(e1, e2);
   const fv3 rs = c - sp, rl = c - lp;
-  const float kn = -1.f / dot(n, n);
-  const float krs = -4.f / (3.f * dot(rs, rs)), krl = -4.f / (3.f * dot(rl, rl));
-  const float kw = 1.f / (3.f * rs.z) + 1.f / (3.f * rl.z);
-  const float knrs = 1.f / dot(n, rs), knrl = 1.f / dot(n, rl);
+  const float kn = vdiv(-1.f, dot(n, n));
+  const float krs = vdiv(-4.f, 3.f * dot(rs, rs)), krl = vdiv(-4.f, 3.f * dot(rl, rl));
+  const float kw = vdiv(1.f, 3.f * rs.z) + vdiv(1.f, 3.f * rl.z);
+  const float knrs = vdiv(1.f, dot(n, rs)), knrl = vdiv(1.f, dot(n, rl));
   const fv3 w = kn * n + knrs * rs + knrl * rl;
   const fv3 g1 = cross(e2, w), g2 = cross(w, e1);
   const fv3 common = krs * rs + krl * rl + ((knrs + knrl) * (1.f / 3.f)) * n + mkv(0.f, 0.f, kw);
   const fv3 da0 = alpha * (common - g1 - g2);
   const fv3 da1 = alpha * (common + g1);
   const fv3 da2 = alpha * (common + g2);
-  const float dadm = alpha / rho;
+  const float dadm = vdiv(alpha, rho);
   if (q.bin[0] == q.bin[2]) {
     const float g = __ldg(col + (size_t)q.bin[0] * stride);
     dv[0] = g * da0;
@@ -277,12 +277,12 @@ __device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3
   TentGrad tgr;
   tent_grad(col, stride, T, q.c, q.bin, tgr);
   const float span = q.c[2] - q.c[0];
-  const float kk = -2.f / (bw * span * span);
+  const float kk = vdiv(-2.f, bw * span * span);
   fv3 dc[3];
   for (int k = 0; k < 3; ++k)
-    dc[k] = (1.f / (bw * q.dl[k])) * (q.v[k] - lp) + (1.f / (bw * q.ds[k])) * (q.v[k] - sp);
-  const fv3 dyc0 = kk * ((1.f / -q.dl[0]) * (q.v[0] - lp) + (1.f / -q.ds[0]) * (q.v[0] - sp));
-  const fv3 dyc2 = kk * ((1.f / q.dl[2]) * (q.v[2] - lp) + (1.f / q.ds[2]) * (q.v[2] - sp));
+    dc[k] = vdiv(1.f, bw * q.dl[k]) * (q.v[k] - lp) + vdiv(1.f, bw * q.ds[k]) * (q.v[k] - sp);
+  const fv3 dyc0 = kk * (vdiv(-1.f, q.dl[0]) * (q.v[0] - lp) + vdiv(-1.f, q.ds[0]) * (q.v[0] - sp));
+  const fv3 dyc2 = kk * (vdiv(1.f, q.dl[2]) * (q.v[2] - lp) + vdiv(1.f, q.ds[2]) * (q.v[2] - sp));
   dv[0] = tgr.part0 * da0 + alpha * (tgr.ayc * dyc0 + tgr.a0 * dc[0]);
   dv[1] = tgr.part0 * da1 + alpha * (tgr.a1 * dc[1]);
   dv[2] = tgr.part0 * da2 + alpha * (tgr.ayc * dyc2 + tgr.a2 * dc[2]);

@@ -35,6 +35,12 @@ struct Hist {
   __device__ __forceinline__ void add(int b, float v) const { atomicAdd(h + b * TS + sl, v); }
 };
 
+// Division for values that decide nothing (tent heights, gradient factors,
+// alpha): the hardware reciprocal and one multiply, within 2 ulp, instead of
+// the correctly rounded division sequence. Bins and vertex order never pass
+// through it.
+__device__ __forceinline__ float vdiv(float a, float b) { return __fdividef(a, b); }
+
 // DrawTrapezoid (mesh_common.h:61-94): integrates the line through
 // (ca, ya) - (cb, yb) over each bin it spans (midpoint rule, exact for a line).
 template <class H>
@@ -44,7 +50,7 @@ __device__ __forceinline__ void splat_segment(const H& h, float ca, int ba, floa
     if (h.in(ba)) h.add(ba, 0.5f * (cb - ca) * (ya + yb));
     return;
   }
-  const float slope = (yb - ya) / (cb - ca);
+  const float slope = vdiv(yb - ya, cb - ca);
   if (h.in(ba)) {
     const float w = (float)(ba + 1) - ca;
     h.add(ba, w * (ya + 0.5f * w * slope));
@@ -67,7 +73,7 @@ __device__ __forceinline__ void splat_tent(const H& h, const float c[3], const i
     h.add(bin[0], alpha);
     return;
   }
-  const float yc = 2.f * alpha / (c[2] - c[0]);
+  const float yc = vdiv(2.f * alpha, c[2] - c[0]);
   splat_segment(h, c[0], bin[0], 0.f, c[1], bin[1], yc);
   splat_segment(h, c[1], bin[1], yc, c[2], bin[2], 0.f);
 }
@@ -124,7 +130,7 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
     }
     return;
   }
-  const float inv = 1.f / (cb - ca);
+  const float inv = vdiv(1.f, cb - ca);
   const float slope = (yb - ya) * inv;
   const float q = slope * inv;
   if (in(ba)) {
@@ -163,7 +169,7 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
 
 __device__ __forceinline__ void tent_grad(const float* __restrict__ col, int64_t stride, int T,
                                           const float c[3], const int bin[3], TentGrad& out) {
-  const float yc = 2.f / (c[2] - c[0]);
+  const float yc = vdiv(2.f, c[2] - c[0]);
   float part0 = 0.f;
   SegSums s1{0.f, 0.f, 0.f, 0.f}, s2{0.f, 0.f, 0.f, 0.f};
   grad_segment(col, stride, T, part0, s1, c[0], bin[0], 0.f, c[1], bin[1], yc);
