@@ -233,7 +233,7 @@ __device__ __forceinline__ float alpha_confocal(const ConfocalPair& q, fv3 c, fv
   if (!(r.z > 0.f)) return 0.f;
   const float nr = dot(n, r), rr = dot(r, r), nn = dot(n, n);
   const float rr2 = rr * rr;
-  return vdiv(100.f * rho * (r.z * r.z) * (nr * nr), sqrtf(nn) * (rr2 * rr2));
+  return vdiv(100.f * rho * (r.z * r.z) * (nr * nr) * rsqrtf(nn), rr2 * rr2);
 }
 
 template <int TS>

@@ -104,8 +104,9 @@ __device__ __forceinline__ float alpha_exhaustive(const ExhPair& q, fv3 c, fv3 s
   const fv3 rs = c - sp, rl = c - lp;
   if (!(rs.z > 0.f) || !(rl.z > 0.f)) return 0.f;
   const float rss = dot(rs, rs), rll = dot(rl, rl);
-  return vdiv(100.f * rho * rs.z * rl.z * fabsf(dot(n, rs)) * fabsf(dot(n, rl)),
-              sqrtf(dot(n, n)) * (rss * rss) * (rll * rll));
+  return vdiv(100.f * rho * rs.z * rl.z * fabsf(dot(n, rs)) * fabsf(dot(n, rl)) *
+                  rsqrtf(dot(n, n)),
+              (rss * rss) * (rll * rll));
 }
 
 __device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int l, fv3 sp,

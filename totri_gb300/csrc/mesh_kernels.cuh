@@ -37,8 +37,9 @@ struct Hist {
 
 // Division for values that decide nothing (tent heights, gradient factors,
 // alpha): the hardware reciprocal and one multiply, within 2 ulp, instead of
-// the correctly rounded division sequence. Bins and vertex order never pass
-// through it.
+// the correctly rounded division sequence (alpha's 1/|n| is likewise the
+// hardware reciprocal square root). Bins and vertex order never pass through
+// it.
 __device__ __forceinline__ float vdiv(float a, float b) { return __fdividef(a, b); }
 
 // DrawTrapezoid (mesh_common.h:61-94): integrates the line through
