@@ -236,8 +236,8 @@ def secondary_metrics(device, flush, reps=5):
     """The other throughputs named by the headline metric, on the 128^3 workloads:
     Velten backprojection (128^3 voxels x 128x128 scan points x 1024 bins),
     volume render + exact adjoint, RBF splat + gradient (4096 Gaussians),
-    marching cubes + gradient on that RBF volume, a pose fit and f-k
-    migration."""
+    marching cubes + gradient on that RBF volume, a pose fit, f-k
+    migration and a shaded 512x512 preview of a 20,480-face mesh."""
     from totri_gb300 import scenes
     from totri_gb300.totri_cpp import reconstruct as K
     from totri_gb300.totri_cpp import render as R
@@ -287,7 +287,16 @@ def secondary_metrics(device, flush, reps=5):
     fk_in = torch.rand((1, 512, 64, 64), device=device) ** 4
     fk = FkMigration(512 * 0.005, 2.0, 2.0)
     ms_fk = _timed(lambda: fk(fk_in), flush, reps)
+    from totri_gb300.util import UnitCubeMeshRender
+    pv, pf, _ = scenes.displaced_sphere(5, 1)
+    pv, pf = pv[0].to(device), pf[0].to(device)
+    preview = UnitCubeMeshRender(resolution=512)
+    ms_pv = _timed(lambda: preview.apply(pv, pf), flush, reps)
     return {
+        "preview images/s": {"value": 1e3 / ms_pv, "ms": ms_pv,
+                             "workload": "UnitCubeMeshRender 512x512 of a 20,480-face mesh "
+                                         "(vertex normals, projection, raster, Phong shading; "
+                                         "allocation of the image included)"},
         "fk migration voxels/s": {"value": 512 * 64 * 64 / (ms_fk / 1e3), "ms": ms_fk,
                                   "workload": "512 bins x 64 x 64 scan points (2 x 512 x 64 x "
                                               "64 complex FFTs, cuFFT through torch.fft)"},

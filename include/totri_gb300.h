@@ -424,6 +424,43 @@ int totri_depth_raster(const totri_array_t* verts, const totri_array_t* faces,
                        void* workspace, size_t workspace_bytes, void* stream);
 
 /* ----------------------------------------------------------------------- */
+/* util: shaded perspective preview renderer                                */
+
+/* Camera, light, material and blend settings of totri_shaded_raster. View
+ * coordinates are row vectors: view = world @ rotation + translation
+ * (rotation row-major [3][3]); normalised device coordinates are
+ * ndc.x = focal[0] * view.x / view.z, ndc.y = focal[1] * view.y / view.z. */
+typedef struct totri_shading {
+  float rotation[9];
+  float translation[3];
+  float focal[2];
+  float znear, zfar;          /* depth range of the blend weights            */
+  float camera_center[3];     /* world position of the eye (specular term)   */
+  float light_location[3];    /* one point light                             */
+  float light_ambient[3], light_diffuse[3], light_specular[3];
+  float material_ambient[3], material_diffuse[3], material_specular[3];
+  float shininess;
+  float background[3];
+  float sigma, gamma;         /* blend sharpness (coverage, depth)           */
+} totri_shading_t;
+
+/* Replaces totri.util.render.UnitCubeMeshRender.apply (totri/util/render.py:
+ * 17-81: pytorch3d FoVPerspectiveCameras, one face per pixel without blur,
+ * SoftPhongShader with a point light and vertex colours): verts [V,3] float32,
+ * faces [F,3] int64 (a face with an index outside [0, V) is skipped), colors
+ * [V,3] float32 (any strides, e.g. a broadcast row) -> image [3,H,W] float32,
+ * and when pix_to_face is not NULL the winning face per pixel [H,W] int32
+ * (-1 where empty). Pixel (row r, column c) samples ndc
+ * x = -1 + (2 (W-1-c) + 1) / W, y = -1 + (2 (H-1-r) + 1) / H (the longer side
+ * scaled by its ratio to the shorter). Scratch:
+ * totri_shaded_raster_workspace(V, H, W) bytes. */
+size_t totri_shaded_raster_workspace(int64_t num_verts, int64_t height, int64_t width);
+int totri_shaded_raster(const totri_array_t* verts, const totri_array_t* faces,
+                        const totri_array_t* colors, const totri_shading_t* shading,
+                        const totri_array_t* image, const totri_array_t* pix_to_face,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* ----------------------------------------------------------------------- */
 /* util: differentiable marching cubes                                      */
 
 /* Replaces tomcubes.MarchingCubesFunction (an un-vendored submodule of the

@@ -425,3 +425,9 @@ from .fk import fk_migration, stolt  # noqa: E402,F401
 # Orthographic depth rasteriser (numpy restatement).
 
 from .raster import depth_raster  # noqa: E402,F401
+
+
+# ---------------------------------------------------------------------------
+# Shaded perspective preview rasteriser (numpy restatement).
+
+from .shading import shaded_raster  # noqa: E402,F401

@@ -40,6 +40,30 @@ class Array(ctypes.Structure):
     ]
 
 
+class Shading(ctypes.Structure):
+    """totri_shading_t: camera, light, material and blend settings of the
+    shaded preview rasteriser."""
+    _fields_ = [
+        ("rotation", ctypes.c_float * 9),
+        ("translation", ctypes.c_float * 3),
+        ("focal", ctypes.c_float * 2),
+        ("znear", ctypes.c_float),
+        ("zfar", ctypes.c_float),
+        ("camera_center", ctypes.c_float * 3),
+        ("light_location", ctypes.c_float * 3),
+        ("light_ambient", ctypes.c_float * 3),
+        ("light_diffuse", ctypes.c_float * 3),
+        ("light_specular", ctypes.c_float * 3),
+        ("material_ambient", ctypes.c_float * 3),
+        ("material_diffuse", ctypes.c_float * 3),
+        ("material_specular", ctypes.c_float * 3),
+        ("shininess", ctypes.c_float),
+        ("background", ctypes.c_float * 3),
+        ("sigma", ctypes.c_float),
+        ("gamma", ctypes.c_float),
+    ]
+
+
 _ArrP = ctypes.POINTER(Array)
 _F3 = ctypes.c_float * 3
 _vp = ctypes.c_void_p
@@ -91,6 +115,9 @@ _SIGNATURES = {
     "totri_rbf2volume_gaussian_grad": [_ArrP] * 4 + [_F3, _F3, _vp],
     "totri_depth_raster_workspace": [_i64, _i64],
     "totri_depth_raster": [_ArrP] * 4 + [_flt] * 6 + [_vp, _sz, _vp],
+    "totri_shaded_raster_workspace": [_i64, _i64, _i64],
+    "totri_shaded_raster": [_ArrP, _ArrP, _ArrP, ctypes.POINTER(Shading), _ArrP, _ArrP, _vp,
+                            _sz, _vp],
     "totri_fk_prepare": [_ArrP, _ArrP, _vp],
     "totri_fk_stolt": [_ArrP, _ArrP, _flt, _flt, _flt, _int, _int, _vp],
     "totri_fk_finish": [_ArrP, _ArrP, _vp],
@@ -109,6 +136,7 @@ _RESTYPES = {
     "totri_volume_workspace": ctypes.c_size_t,
     "totri_marching_cubes_workspace": ctypes.c_size_t,
     "totri_depth_raster_workspace": ctypes.c_size_t,
+    "totri_shaded_raster_workspace": ctypes.c_size_t,
     "totri_profile_reset": None,
 }
 
