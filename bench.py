@@ -561,6 +561,55 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
+def reference_gpu_secondary(device, reps=2):
+    """The reference's own volume, backprojection and RBF kernels (its sources
+    compiled for sm_103a, launched with its launchers' geometry) timed on the
+    workloads of the secondary lines, on the same GPU."""
+    from oracle import ref_gpu
+    from totri_gb300 import scenes
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    s = scenes.volume_scene()
+    vd, bd = s["volume_def"], s["bin_def"]
+    sp = s["scan_points"].to(device).contiguous()
+    S = sp.shape[1]
+    nvox = int(np.prod(vd.resolution))
+    tr = torch.rand((1, bd.num, S), device=device)
+    vol_out = torch.empty((1,) + tuple(vd.resolution), device=device)
+    empty = torch.zeros((1, 0, 3), device=device)
+    ms_bp = _timed(lambda: ref_gpu.backprojection_confocal_velten(
+        tr, sp, empty, vol_out, vd.start, vd.end, bd.width, bd.offset), flush, reps, warmup=1)
+    vol = s["volume"].to(device).contiguous()
+    mp = sp[0].T.contiguous()
+    size = tuple(e - a for a, e in zip(vd.start, vd.end))
+    trv = torch.empty((S, bd.num), device=device)
+    ms_vf = _timed(lambda: ref_gpu.volume_confocal_forward(vol, mp, trv, vd.start, size,
+                                                           bd.width, bd.offset),
+                   flush, reps, warmup=1)
+    adj = torch.empty_like(vol)
+    ms_va = _timed(lambda: ref_gpu.volume_confocal_grad_volume(adj, mp, trv, vd.start, size,
+                                                               bd.width, bd.offset),
+                   flush, reps, warmup=1)
+    rbf = scenes.rbf_set(4096, seed=5).to(device).contiguous()
+    rvol = torch.empty((1, 2) + tuple(vd.resolution), device=device)
+    ms_rf = _timed(lambda: ref_gpu.rbf2volume_forward(rbf, rvol, vd.start, vd.end), flush,
+                   reps, warmup=1)
+    rgrad = torch.empty_like(rbf)
+    vg = torch.randn_like(rvol)
+    ms_rg = _timed(lambda: ref_gpu.rbf2volume_grad(rbf, rvol, vg, rgrad, vd.start, vd.end),
+                   flush, reps, warmup=1)
+    pairs = nvox * S
+    return {
+        "backproj voxel·scanpt/s": {"value": pairs / (ms_bp / 1e3), "ms": ms_bp},
+        "volume render voxel·scanpt/s": {"value": pairs / (ms_vf / 1e3), "ms": ms_vf},
+        "volume adjoint voxel·scanpt/s": {
+            "value": pairs / (ms_va / 1e3), "ms": ms_va,
+            "note": "the reference's transposed operator (its volume backward)"},
+        "rbf2volume voxel·gaussian/s": {"value": nvox * 4096 / (ms_rf / 1e3), "ms": ms_rf},
+        "rbf2volume grad voxel·gaussian/s": {"value": nvox * 4096 / (ms_rg / 1e3),
+                                             "ms": ms_rg},
+    }
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -591,7 +640,14 @@ def run_reference(args, world, rank):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference mesh path needs the OptiX SDK (absent); this arm runs the "
                 "CPU restatement of its algorithm",
+        "secondary": None,
     }
+    from oracle import ref_gpu
+    if not args.no_secondary and ref_gpu.available():
+        line["secondary"] = reference_gpu_secondary(torch.device("cuda", 0))
+        line["secondary_note"] = ("the reference's own volume, backprojection and RBF CUDA "
+                                  "kernels, built from its sources for sm_103a, on the "
+                                  "workloads of this bench's secondary lines, same GPU")
     print(json.dumps(line), flush=True)
 
 

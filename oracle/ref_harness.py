@@ -25,6 +25,7 @@ OUT = os.path.join(HERE, "_ref")
 GEN = os.path.join(OUT, "gen")
 REF_SRC = os.path.join(os.environ.get("TOTRI_REFERENCE", "/root/reference"), "src")
 LIB = os.path.join(OUT, "libref_kernels.so")
+CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 
 CXX = ["g++", "-std=c++20", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-w",
        "-include", os.path.join(STUBS, "cuda_host_shim.h"), "-I" + STUBS,
@@ -112,6 +113,21 @@ def build(force=False):
     _run(["g++", "-shared", "-fopenmp", "-o", LIB + ".tmp", *objs])
     os.replace(LIB + ".tmp", LIB)
     return LIB
+
+
+def build_gpu(force=False):
+    """Compiles the reference's volume, backprojection and RBF kernels for
+    sm_103a (oracle/ref_harness/gpu_kernels.cu around the kernel functions cut
+    out by build()) into oracle/_ref/ref_kernels.cubin: a device-only image,
+    loaded on a GPU machine through the CUDA driver (oracle/ref_gpu.py)."""
+    build(force)
+    src = os.path.join(HARNESS, "gpu_kernels.cu")
+    if os.path.exists(CUBIN) and not force and os.path.getmtime(CUBIN) >= os.path.getmtime(src):
+        return CUBIN
+    _run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-cubin",
+          "-I" + REF_SRC, "-I" + GEN, src, "-o", CUBIN + ".tmp"])
+    os.replace(CUBIN + ".tmp", CUBIN)
+    return CUBIN
 
 
 _lib = None
