@@ -47,7 +47,7 @@ def test_visibility_modes_agree_under_occlusion(cuda_lib):
     verts, faces, sp = _occluded_scene()
     d = [t.cuda() for t in (verts, faces, sp)]
     ref = oracle.mesh_visibility(verts[0].numpy(), faces[0].numpy(), sp[0].numpy())
-    for mode in (0, 1, 2, 3, 4, 5, 6):  # 0: the built-in choice
+    for mode in (0, 1, 2, 3, 4, 5, 6, 7):  # 0: the built-in choice
         assert np.array_equal(_masks(*d, mode=mode), ref), mode
     assert np.array_equal(_masks(*d, brute=True), ref)
     assert 0.05 < ref.mean() < 0.5
@@ -57,7 +57,7 @@ def test_visibility_modes_agree_full_size(cuda_lib):
     s = scenes.confocal_differentiable()
     d = [s[k].cuda() for k in ("verts", "faces", "scan_points")]
     ray = _masks(*d, mode=1)
-    for mode in (0, 2, 3, 5, 6):
+    for mode in (0, 2, 3, 5, 6, 7):
         assert np.array_equal(_masks(*d, mode=mode), ray), mode
 
 

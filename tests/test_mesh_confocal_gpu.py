@@ -298,6 +298,40 @@ def test_seeded_visibility_equals_brute_force(cuda_lib):
         assert torch.equal(got, bf), case
 
 
+def _with_keys(keys, fn):
+    from totri_gb300 import autotune
+    for k, v in keys.items():
+        autotune.set_tile(k, v)
+    try:
+        return fn()
+    finally:
+        for k in keys:
+            autotune.set_tile(k, 0)
+
+
+def test_shaft_visibility_equals_brute_force(cuda_lib):
+    """The shaft search (one warp-wide BVH walk per target over the hull of
+    the warp's wall points and the target's hit box, then exact tests of its
+    candidates per lane) gives the brute-force masks bit for bit: with the
+    surface walk on or off, with the candidate list capped to force the
+    per-lane fallback, and with the wall 40 m away."""
+    s = scenes.confocal_differentiable()
+    d = _dev(s)
+    bf = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
+    for seed, cap in ((0, 0), (1, 0), (0, 1), (2, 5)):
+        got = _with_keys({"mesh.visibility.mode": 7, "mesh.visibility.seed": seed,
+                          "mesh.visibility.shaft.cap": cap},
+                         lambda: R.mesh_visibility(d["verts"], d["faces"], d["scan_points"]))
+        assert torch.equal(got, bf), (seed, cap)
+    far = d["scan_points"].clone()
+    far[..., 2] = -40.0
+    far[..., :2] *= 20.0
+    bf = R.mesh_visibility(d["verts"], d["faces"], far, brute_force=True)
+    got = _with_keys({"mesh.visibility.mode": 7},
+                     lambda: R.mesh_visibility(d["verts"], d["faces"], far))
+    assert torch.equal(got, bf)
+
+
 def test_seeded_visibility_without_or_with_odd_adjacency(cuda_lib):
     """Edge adjacency only steers the walk: a triangle soup (no shared vertex
     indices), non-manifold fins (three faces on one edge) and degenerate faces

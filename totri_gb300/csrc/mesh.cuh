@@ -397,20 +397,24 @@ __device__ __forceinline__ int surface_walk(const Scene& sc, int b, int n, int k
 // With seed_steps > 0 and a seed face (seed >= 0), the targets that seed_mode
 // selects first try surface_walk from the seed; `seed` returns the occluder
 // found by either search, for the next query.
-__device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
-                                                  const Target& tg, fv3 o, uint32_t* status,
-                                                  int& seed, int seed_mode, int seed_steps) {
-  constexpr int kDone = INT_MIN;  // below every leaf code ~k, k < n
-  const int k = tg.k;
+// The part of a query that needs no search: the ray to the target's centroid,
+// the target's own hit and, for the targets that seed_mode selects, the
+// surface walk from `seed`. Returns 1 when an occluder search must still
+// decide (dir, tmax and tf set), else 0 with the answer in `vis`.
+__device__ __forceinline__ int query_prefix(const Scene& sc, int b, int n, const Target& tg,
+                                            fv3 o, int& seed, int seed_mode, int seed_steps,
+                                            fv3& dir, float& tmax, float& tf, bool& vis) {
+  vis = false;
   const fv3 D = xsub3(tg.c, o);
   const float dist = xlen(D);
-  if (!(dist >= 1e-6f)) return false;
-  const fv3 dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
-  const float tmax = xadd(xmul(dist, 1.01f), 1e-3f);
-  const int f = tg.f;
-  float tf;
-  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return false;
-  if (n == 1) return true;
+  if (!(dist >= 1e-6f)) return 0;
+  dir = mkv(xdiv(D.x, dist), xdiv(D.y, dist), xdiv(D.z, dist));
+  tmax = xadd(xmul(dist, 1.01f), 1e-3f);
+  if (!tri_hit(tg.a0, tg.a1, tg.a2, tg.a3, o, dir, tmax, tf)) return 0;
+  if (n == 1) {
+    vis = true;
+    return 0;
+  }
   if (seed_steps > 0 && seed >= 0 && seed_mode != kSeedOff) {
     bool walk = seed_mode == kSeedAll;
     if (!walk) {  // faces wound outward and seen from behind are mostly occluded
@@ -418,13 +422,23 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
       walk = (dot(nrm, D) > 0.f) == (seed_mode == kSeedBack);
     }
     if (walk) {
-      const int g = surface_walk(sc, b, n, k, f, seed, o, dir, tmax, tf, seed_steps);
+      const int g = surface_walk(sc, b, n, tg.k, tg.f, seed, o, dir, tmax, tf, seed_steps);
       if (g >= 0) {
         seed = g;
-        return false;
+        return 0;
       }
     }
   }
+  return 1;
+}
+
+// The BVH search of target_visible_pp: true when some face other than the
+// target k (original index f) hits the ray before the target's hit at tf
+// (ties to the lower original index); `seed` returns that occluder.
+__device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int k, int f, fv3 o,
+                                             fv3 dir, float tmax, float tf, uint32_t* status,
+                                             int& seed) {
+  constexpr int kDone = INT_MIN;  // below every leaf code ~k, k < n
   const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
   const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   int stack[64];
@@ -439,7 +453,7 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
     while (node >= 0) {
       if (--budget < 0 || (unsigned)node >= inner) {  // malformed tree
         atomicOr(status, kStatusTraversalCap);
-        return true;
+        return false;
       }
       const float4* nd = nodes + node * 4;
       const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
@@ -477,7 +491,7 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
           if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
               (tq < tf || (tq == tf && __float_as_int(q3.w) < f))) {
             seed = kk;
-            return false;
+            return true;
           }
         }
       }
@@ -488,7 +502,140 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
       }
     }
   }
-  return true;
+  return false;
+}
+
+__device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
+                                                  const Target& tg, fv3 o, uint32_t* status,
+                                                  int& seed, int seed_mode, int seed_steps) {
+  fv3 dir;
+  float tmax, tf;
+  bool vis;
+  if (!query_prefix(sc, b, n, tg, o, seed, seed_mode, seed_steps, dir, tmax, tf, vis))
+    return vis;
+  return !bvh_occluded(sc, b, n, tg.k, tg.f, o, dir, tmax, tf, status, seed);
+}
+
+// Occluder candidates shared by the rays of a warp: the rays start in the box
+// P (the warp's wall points) and end at the target's hit point, inside the
+// target's hit-point box C, so every point of every ray segment lies in the
+// convex hull of P and C, the union over s in [0, 1] of the boxes
+// (1 - s) P + s C. A BVH box meets that hull iff the s-intervals of its six
+// face constraints, each linear in s, intersect within [0, 1]. Both boxes are
+// grown by the hit-point margin delta, far beyond the rounding of this test,
+// and BVH boxes hold a delta margin around every accepted hit point, so a box
+// holding an occluder of any of the rays is never rejected: the candidates
+// include every occluder the rays' own BVH walks would test, and the exact
+// triangle test decides.
+struct Shaft {
+  float plo[3], nplrl[3], rl[3];  // lower face: Plo + s (Clo - Plo) <= box hi
+  float phi[3], nphrh[3], rh[3];  // upper face: Phi + s (Chi - Phi) >= box lo
+  bool lneg[3], hneg[3];
+};
+
+__device__ __forceinline__ Shaft make_shaft(const float plo[3], const float phi[3],
+                                            const float clo[3], const float chi[3]) {
+  Shaft h;
+  for (int a = 0; a < 3; ++a) {
+    const float dl = clo[a] - plo[a], dh = chi[a] - phi[a];
+    h.plo[a] = plo[a];
+    h.phi[a] = phi[a];
+    h.rl[a] = 1.f / dl;
+    h.rh[a] = 1.f / dh;
+    h.nplrl[a] = -(plo[a] * h.rl[a]);
+    h.nphrh[a] = -(phi[a] * h.rh[a]);
+    h.lneg[a] = dl < 0.f;
+    h.hneg[a] = dh < 0.f;
+  }
+  return h;
+}
+
+// Box [lo, hi] against the hull; a NaN bound (a zero extent meeting a box
+// face exactly) drops its constraint, which can only admit a box.
+__device__ __forceinline__ bool shaft_box(const Shaft& h, float lx, float ly, float lz, float hx,
+                                          float hy, float hz) {
+  const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
+  float smin = 0.f, smax = 1.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float u = fmaf(hi[a], h.rl[a], h.nplrl[a]);  // (hi - Plo) / dl
+    const float w = fmaf(lo[a], h.rh[a], h.nphrh[a]);  // (lo - Phi) / dh
+    if (h.lneg[a]) smin = fmaxf(smin, u);
+    else smax = fminf(smax, u);
+    if (h.hneg[a]) smax = fminf(smax, w);
+    else smin = fmaxf(smin, w);
+  }
+  return smin <= smax;
+}
+
+// Warp-collective breadth-first walk of the BVH restricted to the hull: each
+// round the lanes test the children of up to 32 frontier nodes at once.
+// Writes the candidate leaves (Morton positions, the target k excluded) to
+// cand and returns their count, or -1 when a frontier overflows its capacity,
+// the candidates exceed cap (at most kCand) or the tree is malformed (the
+// caller then searches per lane). All 32 lanes must call it with the same
+// arguments.
+template <int kFrontier, int kCand>
+__device__ __forceinline__ int shaft_candidates(const Scene& sc, int b, int n, int k,
+                                                const Shaft& h, int* fr0, int* fr1, int* cand,
+                                                int lane, int cap) {
+  const float4* nodes = sc.nodes + (size_t)b * sc.F * 4;
+  const unsigned inner = (unsigned)(n - 1);
+  const unsigned lt = (1u << lane) - 1u;
+  if (lane == 0) fr0[0] = 0;
+  __syncwarp();
+  int* cur = fr0;
+  int* nxt = fr1;
+  int cnt = 1, nc = 0;
+  bool bad = false;
+  for (int round = 0; cnt > 0; ++round) {
+    if (round >= 96) return -1;
+    int ncnt = 0;
+    for (int base = 0; base < cnt; base += 32) {
+      const int idx = base + lane;
+      bool h0 = false, h1 = false;
+      int c0 = 0, c1 = 0;
+      if (idx < cnt) {
+        const int node = cur[idx];
+        if ((unsigned)node < inner) {
+          const float4* nd = nodes + node * 4;
+          const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2),
+                       n3 = __ldg(nd + 3);
+          h0 = shaft_box(h, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+          h1 = shaft_box(h, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+          c0 = __float_as_int(n3.x);
+          c1 = __float_as_int(n3.y);
+        } else {
+          bad = true;
+        }
+      }
+      const bool i0 = h0 && c0 >= 0, i1 = h1 && c1 >= 0;
+      const bool l0 = h0 && c0 < 0 && ~c0 != k, l1 = h1 && c1 < 0 && ~c1 != k;
+      const unsigned bi0 = __ballot_sync(0xffffffffu, i0), bi1 = __ballot_sync(0xffffffffu, i1);
+      const unsigned bl0 = __ballot_sync(0xffffffffu, l0), bl1 = __ballot_sync(0xffffffffu, l1);
+      int pi = ncnt + __popc(bi0 & lt) + __popc(bi1 & lt);
+      if (i0) {
+        if (pi < kFrontier) nxt[pi] = c0;
+        ++pi;
+      }
+      if (i1 && pi < kFrontier) nxt[pi] = c1;
+      ncnt += __popc(bi0) + __popc(bi1);
+      int pl = nc + __popc(bl0 & lt) + __popc(bl1 & lt);
+      if (l0) {
+        if (pl < kCand) cand[pl] = ~c0;
+        ++pl;
+      }
+      if (l1 && pl < kCand) cand[pl] = ~c1;
+      nc += __popc(bl0) + __popc(bl1);
+    }
+    __syncwarp();
+    if (__any_sync(0xffffffffu, bad) || ncnt > kFrontier || nc > cap) return -1;
+    int* t = cur;
+    cur = nxt;
+    nxt = t;
+    cnt = ncnt;
+  }
+  return nc;
 }
 
 // target_visible_pp over the 4-wide tree: each binary node at even depth
