@@ -22,6 +22,7 @@ namespace {
 constexpr int kSortThreads = 1024;
 constexpr int kSortBits = 10;
 constexpr int kSortDigits = 1 << kSortBits;
+constexpr int kSortUnroll = 4;  // batches of 32 keys loaded ahead per warp
 
 __global__ void init_kernel(Scene sc, int F) {
   const int b = blockIdx.y;
@@ -146,35 +147,58 @@ __global__ void morton_kernel(Scene sc, BuildInputs in) {
   sc.vals[base + f] = (uint32_t)f;
 }
 
-// Stable LSD radix sort of n (key, value) pairs, 3 passes of 10 bits, one CTA
-// of 1024 threads per mesh. Ranks within a tile of 1024 keys come from
-// warp-level digit matching plus a per-digit scan across the 32 warps.
-// One-CTA LSD radix sort of n 30-bit keys with their values: three 10-bit
-// passes k0/v0 -> k1/v1 -> k0/v0 -> k1/v1, so the sorted pairs end in k1/v1.
-// Stable; ranks within a warp come from __match_any_sync.
+// One-CTA stable LSD radix sort of n 30-bit keys with their values: three
+// 10-bit passes k0/v0 -> k1/v1 -> k0/v0 -> k1/v1, so the sorted pairs end in
+// k1/v1. Warp w owns the w-th of 32 contiguous chunks of the input. A pass
+// counts each warp's digits (wcount[w][digit]), turns the counts into each
+// warp's first output position per digit with one scan over the warps and one
+// over the digits, and then lets every warp scatter its chunk in order, 32
+// keys at a time, ranking equal digits within the batch with
+// __match_any_sync. Warps own ordered ranges and keep their batches in order,
+// so the sort is stable.
 __device__ void cta_radix_sort30(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, int n,
                                  uint32_t* smem) {
-  uint32_t* wcount = smem;                        // [32][1024]
-  uint32_t* offset = smem + 32 * kSortDigits;     // [1024] running digit offset
-  uint32_t* total = offset + kSortDigits;         // [1024] digit count in tile
+  uint32_t* wcount = smem;                     // [32][1024] per-warp digit count, then cursor
+  uint32_t* offset = smem + 32 * kSortDigits;  // [1024] first position of each digit
+  uint32_t* total = offset + kSortDigits;      // [1024] digit totals; [32] scan partials
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < 32 * kSortDigits; i += kSortThreads) wcount[i] = 0;
+  const uint32_t lt = (1u << lane) - 1u;
+  const int chunk = (((n + 31) / 32) + 31) & ~31;
+  const int lo = min(n, warp * chunk), hi = min(n, lo + chunk);
+  uint32_t* mine = wcount + warp * kSortDigits;
   for (int pass = 0; pass < 3; ++pass) {
     const int shift = pass * kSortBits;
     const uint32_t* ksrc = (pass & 1) ? k1 : k0;
     const uint32_t* vsrc = (pass & 1) ? v1 : v0;
     uint32_t* kdst = (pass & 1) ? k0 : k1;
     uint32_t* vdst = (pass & 1) ? v0 : v1;
-    // histogram into offset[]
-    offset[tid] = 0;
+    for (int d = lane; d < kSortDigits; d += 32) mine[d] = 0;
+    __syncwarp();
+    for (int base = lo; base < hi; base += 32 * kSortUnroll) {
+      uint32_t key[kSortUnroll];  // loads of kSortUnroll batches in flight together
+#pragma unroll
+      for (int u = 0; u < kSortUnroll; ++u) {
+        const int i = base + 32 * u + lane;
+        key[u] = i < hi ? ksrc[i] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kSortUnroll; ++u) {
+        const bool valid = base + 32 * u + lane < hi;
+        const uint32_t digit = valid ? ((key[u] >> shift) & (kSortDigits - 1)) : kSortDigits;
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        if (valid && lane == __ffs(peers) - 1) mine[digit] += __popc(peers);
+        __syncwarp();
+      }
+    }
     __syncthreads();
-    for (int i = tid; i < n; i += kSortThreads)
-      atomicAdd(&offset[(ksrc[i] >> shift) & (kSortDigits - 1)], 1u);
-    __syncthreads();
-    // exclusive scan of offset[] (1024 entries, one per thread)
-    {
-      const uint32_t x = offset[tid];
-      uint32_t incl = x;
+    {  // digit tid: exclusive prefix over the warps, then over the digits
+      uint32_t run = 0;
+      for (int w = 0; w < 32; ++w) {
+        const uint32_t c = wcount[w * kSortDigits + tid];
+        wcount[w * kSortDigits + tid] = run;
+        run += c;
+      }
+      uint32_t incl = run;
       for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
@@ -191,39 +215,33 @@ __device__ void cta_radix_sort30(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint3
         total[lane] = wi - w;
       }
       __syncthreads();
-      offset[tid] = total[warp] + incl - x;
+      offset[tid] = total[warp] + incl - run;
       __syncthreads();
     }
-    for (int base = 0; base < n; base += kSortThreads) {
-      const int i = base + tid;
-      const bool valid = i < n;
-      const uint32_t key = valid ? ksrc[i] : 0u;
-      const uint32_t val = valid ? vsrc[i] : 0u;
-      const uint32_t digit = valid ? ((key >> shift) & (kSortDigits - 1)) : kSortDigits;
-      const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-      const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-      const int leader = __ffs(peers) - 1;
-      if (valid && lane == leader) wcount[warp * kSortDigits + digit] = __popc(peers);
-      __syncthreads();
-      {  // scan over warps for digit tid
-        uint32_t run = 0;
-        for (int w = 0; w < 32; ++w) {
-          const uint32_t c = wcount[w * kSortDigits + tid];
-          wcount[w * kSortDigits + tid] = run;
-          run += c;
+    for (int base = lo; base < hi; base += 32 * kSortUnroll) {
+      uint32_t key[kSortUnroll], val[kSortUnroll];
+#pragma unroll
+      for (int u = 0; u < kSortUnroll; ++u) {
+        const int i = base + 32 * u + lane;
+        key[u] = i < hi ? ksrc[i] : 0u;
+        val[u] = i < hi ? vsrc[i] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kSortUnroll; ++u) {
+        const bool valid = base + 32 * u + lane < hi;
+        const uint32_t digit = valid ? ((key[u] >> shift) & (kSortDigits - 1)) : kSortDigits;
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t cur = 0;
+        if (valid) {
+          cur = mine[digit];
+          const uint32_t pos = offset[digit] + cur + __popc(peers & lt);
+          kdst[pos] = key[u];
+          vdst[pos] = val[u];
         }
-        total[tid] = run;
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) mine[digit] = cur + __popc(peers);
+        __syncwarp();
       }
-      __syncthreads();
-      if (valid) {
-        const uint32_t pos = offset[digit] + wcount[warp * kSortDigits + digit] + rank;
-        kdst[pos] = key;
-        vdst[pos] = val;
-      }
-      __syncthreads();
-      offset[tid] += total[tid];
-      for (int w = 0; w < 32; ++w) wcount[w * kSortDigits + tid] = 0;
-      __syncthreads();
     }
     __syncthreads();
   }

@@ -112,8 +112,10 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
 // one mask word per point and chunk. This is the default visibility kernel.
 constexpr int kMaxPatchChunks = 16;
 
-template <int kWalk>  // 0: target_visible_pp, 1: packet_visible, 2: target_visible_pp4, 3: shaft search
-__global__ void __launch_bounds__(256) visibility_patch_kernel(Scene sc, View3f pts, int P,
+// kWalk 0: target_visible_pp, 1: packet_visible, 2: target_visible_pp4, 3: shaft
+// search; kOcc: CTAs per SM that the register allocation must allow.
+template <int kWalk, int kOcc = 1>
+__global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, View3f pts, int P,
                                                                int row0, int chunks,
                                                                int seed_mode, int seed_steps,
                                                                int shaft_cap) {
@@ -634,9 +636,20 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
       TOTRI_KERNEL("mesh visibility", stream,
                    visibility_patch_kernel<3><<<grid, 256, 0, stream>>>(
                        sc, pts, P, row0, chunks, seed_mode, seed_steps, shaft_cap));
+    // Registers capped for 5 CTAs per SM (48 a thread, 28 bytes of spills):
+    // 8.84 ms against 9.33 ms uncapped (60 registers, 4 CTAs) and 9.03 ms at
+    // 6 CTAs (40 registers) inside the differentiable 20,480-face step.
+    else if (tune::get("mesh.visibility.occupancy") == 1)
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<0, 1><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
+    else if (tune::get("mesh.visibility.occupancy") == 6)
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<0, 6><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
     else
       TOTRI_KERNEL("mesh visibility", stream,
-                   visibility_patch_kernel<0><<<grid, 256, 0, stream>>>(
+                   visibility_patch_kernel<0, 5><<<grid, 256, 0, stream>>>(
                        sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
   }
   return TOTRI_OK;
