@@ -1,16 +1,20 @@
 """The volume, backprojection and RBF operators against the reference's own
 kernels run on the same GPU (oracle/ref_gpu.py: the reference's kernel sources
 compiled for sm_103a and launched with its launchers' geometry) on the same
-seeded inputs. Tolerance: rel-L2 1e-4 (FP32 on both sides). The Velten
-backprojections are the exception: on the GPU the reference takes its lengths
-from CUDA's norm3df (within 2 ulp of the correctly rounded length; the same
-image built without fused multiply-adds gives the same differences), while
-this repo's lengths are the FP32 chain that the oracle and the reference's
-CPU-built golden vectors pin, so a few nearest-bin decisions in a million fall
-on the other side of a bin edge; each such pair moves one voxel by one
-transient sample. Those tests bound the rel-L2 by 1e-3 and require 99.9% of
-the voxels to agree to 1e-5. Skipped where the reference's kernel image has
-not been built (it is built only where the reference tree is present)."""
+seeded inputs. Tolerance: rel-L2 1e-4 (FP32 on both sides), except where the
+reference's GPU build takes a discrete decision from a value rounded by a
+CUDA math function: its squares come from powf(x, 2) and its lengths from
+norm3df (each within 2 ulp of the correctly rounded value; the same image
+built without fused multiply-adds gives the same differences), while this
+repo computes the FP32 chain that the oracle and the reference's CPU-built
+golden vectors pin. A few bin or cell decisions in a million then fall on the
+other side of an edge, each moving one output by one sample (measured on
+these inputs: Velten 10-24 of 32,768 voxels, the transposed volume operator
+4-7 of 32,768, the measurement-point gradient 0-2 of 768; the volume forward
+matches to 2.6e-7). Those checks bound the rel-L2 by 1e-3 and require 99.9%
+(99% for the 768 gradient entries) of the outputs to agree to 1e-5. Skipped
+where the reference's kernel image has not been built (it is built only where
+the reference tree is present)."""
 import numpy as np
 import pytest
 import torch
@@ -31,11 +35,12 @@ def rel(a, b):
     return float(torch.linalg.norm(a - b) / torch.clamp(torch.linalg.norm(b), min=1e-300))
 
 
-def near_bins(ours, ref):
-    """Agreement up to a few pairs on the other side of a bin edge."""
+def near_bins(ours, ref, frac=0.999):
+    """Agreement up to a few samples on the other side of a bin or cell edge:
+    rel-L2 below 1e-3 and all but (1 - frac) of the entries within 1e-5."""
     err = rel(ours, ref)
     close = torch.isclose(ours, ref, rtol=1e-5, atol=1e-5 * float(ref.abs().max()))
-    return err < 1e-3 and float(close.double().mean()) > 0.999
+    return err < 1e-3 and float(close.double().mean()) > frac
 
 
 @pytest.fixture(autouse=True)
@@ -66,11 +71,11 @@ def test_volume_confocal(cuda_lib):
     ours_v, ref_v = torch.empty_like(vol), torch.empty_like(vol)
     R.volume_confocal_grad_volume(ours_v, mp, y, org, size, bw, bo)
     ref_gpu.volume_confocal_grad_volume(ref_v, mp, y, org, size, bw, bo)
-    assert rel(ours_v, ref_v) < 1e-4
+    assert near_bins(ours_v, ref_v), rel(ours_v, ref_v)
     ours_m, ref_m = torch.empty_like(mp), torch.empty_like(mp)
     R.volume_confocal_grad_measurement_points(ours_m, vol, mp, y, org, size, bw, bo)
     ref_gpu.volume_confocal_grad_mp(ref_m, vol, mp, y, org, size, bw, bo)
-    assert rel(ours_m, ref_m) < 1e-4
+    assert near_bins(ours_m, ref_m, 0.99), rel(ours_m, ref_m)
 
 
 def test_volume_exhaustive(cuda_lib):
