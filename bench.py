@@ -40,6 +40,20 @@ FLOP_PER_SEG_FWD = 10.0  # per bin segment of the tent (forward)
 FLOP_PER_SEG_BWD = 60.0  # per bin segment (backward)
 
 
+def algorithmic_bytes(kernel, F, S, T, V):
+    """Bytes one launch must move at least: the visibility walk reads the
+    face records and tree nodes (64 B each) and the wall points and writes one
+    mask bit per (point, face); the splat writes the [T, S] transient; the
+    gradient reads transient_grad and writes vertex and albedo gradients."""
+    if kernel == "mesh visibility":
+        return 64 * F + 64 * (F - 1) + 12 * S + 4 * S * ((F + 31) // 32)
+    if kernel == "mesh confocal splat":
+        return 64 * F + 12 * S + 4 * T * S
+    if kernel == "mesh confocal grad":
+        return 64 * F + 12 * S + 4 * T * S + 16 * V
+    return None
+
+
 def flop_visibility(num_faces):
     """Per-ray BVH visibility model: 2 box tests x 20 per level + 4 triangle tests x 36."""
     return 40.0 * math.ceil(math.log2(max(num_faces, 2))) + 144.0
@@ -727,6 +741,16 @@ def main():
                                "(MEASURED_PEAKS.json holds no FP32 figure)" % (sm_count, max_mhz),
                 "flop_per_pair": flops[dom_name], "pairs_per_launch": pairs,
                 "ms_per_launch": per_launch_ms, "b_bar": bbar}
+        # The same launch against the measured HBM copy bandwidth, from the
+        # bytes it must move: it is far from that roof.
+        alg = algorithmic_bytes(dom_name, F, S, w["bin_def"].num, w["verts"].shape[1])
+        hbm_peak = peaks.get("hbm_gbs")
+        if alg and hbm_peak:
+            ach = alg / (per_launch_ms / 1000.0) / 1e9
+            roof["hbm"] = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                           "frac": ach / hbm_peak, "algorithmic_bytes": alg,
+                           "traffic": roof["traffic"],
+                           "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
     kernels = {k: {"launches": v[0], "ms_per_step": v[2] / args.steps} for k, v in prof.items()}
 
     # End to end through the public API with host buffers.
