@@ -538,7 +538,9 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
     configured = (int)smem;
   }
   // (three CTAs per SM at 80 registers spills and runs 6% slower: 93.5 ms
-  // against 87.8 ms on one 20k-face mesh)
+  // against 87.8 ms on one 20k-face mesh; CTAs of 5 or 6 warps capped at 96
+  // registers for 4 or 3 CTAs per SM spill and took 98 and 95 ms against
+  // 69 ms for this kernel on that mesh)
   const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh exhaustive grad", stream,
                exh_grad_compact_kernel<<<grid, 256, smem, stream>>>(
