@@ -97,3 +97,21 @@ def test_optimizer_schedule():
     assert [lin(i) for i in (0, 2, 4, 9)] == [1.0, 2.0, 3.0, 3.0]
     mul = MultiplicativeInterpolator(1.0, 0.0, 0.5)
     assert [mul(0), mul(0)] == [0.5, 0.25]
+
+
+def test_rbf_fitting_reduce_transient_crops_silent_bins():
+    """Bin cropping of RbfFitting.reduce_transient (reference rbf.py:218-243):
+    bins whose 0.95-quantile stays below a tenth of the largest are cut from
+    both ends, widened by the margin; the bin definition follows."""
+    from totri_gb300.fitting import RbfFitting
+    from totri_gb300.types import BinDef
+    tr = torch.zeros((400, 16))
+    tr[150:201] = torch.linspace(1.0, 2.0, 16)
+    tr[120] = 0.1  # below the threshold: still cropped
+    fit = RbfFitting(BinDef(0.01, 0.5, 400), torch.zeros((16, 3)))
+    out = fit.reduce_transient(tr)
+    assert (fit.bin_def.num, out.shape[0]) == (115, 115)
+    assert abs(fit.bin_def.offset - (0.5 + 0.01 * 118)) < 1e-9
+    assert torch.equal(out, tr[118:233])
+    out = fit.reduce_transient(tr, margin=0)
+    assert out.shape[0] == 51 and torch.equal(out, tr[150:201])

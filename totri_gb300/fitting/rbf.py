@@ -169,6 +169,33 @@ class RbfFitting:
         self.project_transient = project_transient
         self.log_dir = log_dir
 
+    def reduce_transient(self, transient_input, margin=32):
+        """Crops leading and trailing bins without signal (rbf.py:218-243):
+        per bin the 0.95-quantile over the wall points, a threshold of a tenth
+        of the largest such quantile, the first and last bins at or above it
+        widened by `margin`; sets bin_def to the cropped range and returns
+        transient_input [T, S(, L)] cut to it."""
+        q = torch.quantile(transient_input.flatten(start_dim=1), 0.95, dim=1).cpu()
+        threshold = q.max() / 10
+        num_bins = q.shape[0]
+        start, end = 0, num_bins
+        for i in range(num_bins - 1):
+            if q[i] < threshold:
+                start = i + 1
+            else:
+                break
+        for i in range(num_bins - 1, 0, -1):
+            if q[i] < threshold:
+                end = i
+            else:
+                break
+        start = max(start - margin, 0)
+        end = min(end + margin, num_bins)
+        self.bin_def = BinDef(self.bin_def_init.width,
+                              self.bin_def_init.offset + self.bin_def_init.width * start,
+                              end - start)
+        return transient_input[start:end]
+
     # -- loss ---------------------------------------------------------------
 
     def render(self, verts, background_model, transient_input):
