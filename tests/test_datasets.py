@@ -1,8 +1,10 @@
 """MATLAB-format dataset loaders against the reference's own loaders run on
-the same small files (tests/golden/make_golden_datasets.py)."""
+the same small files (tests/golden/make_golden_datasets.py), and the Zaragoza
+loader on a synthetic mapping of its datasets."""
 import os
 
 import numpy as np
+import torch
 
 from totri_gb300.data import OTooleConfocal2018, VeltenNc2012
 
@@ -31,3 +33,43 @@ def test_otoole_confocal2018_matches_reference():
     d.downsample_temporal(4)
     assert np.allclose(d.transient.numpy(), g["otoole_down4"], rtol=1e-6, atol=1e-6)
     assert np.allclose([d.bin_def.width, d.bin_def.offset, d.bin_def.num], g["otoole_bins4"])
+
+
+def _zaragoza_mapping(N=64, H=4, W=5, seed=0):
+    g = np.random.default_rng(seed)
+    x, y = np.meshgrid(np.linspace(-1, 1, W), np.linspace(-1, 1, H))
+    pos = np.stack([x.ravel(), np.zeros(H * W), y.ravel()])  # file frame: the wall at y = 0
+    return {
+        "isConfocal": np.array(1), "deltaT": np.array(0.01), "t0": np.array(0.2),
+        "t": np.array([[N]]), "hiddenVolumePosition": np.array([[0.1], [-1.0], [0.2]]),
+        "hiddenVolumeSize": np.array(0.8), "cameraGridPoints": np.array([[W], [H]]),
+        "cameraGridSize": np.array([[2.0], [2.0]]),
+        "data": g.random((N, 6, H, W)).astype(np.float32),
+        "cameraGridPositions": pos, "cameraGridNormals": np.tile([[0.0], [1.0], [0.0]], H * W),
+        "cameraPosition": np.array([[0.3], [-0.4], [0.5]]),
+    }
+
+
+def test_zaragoza_mapping_layout_and_rectify():
+    """Zaragoza (reference totri/data/zaragoza.py:57-128) from a mapping of
+    its datasets: bins, volume box, summed transient, wall-frame grids, and
+    rectification by the per-column origin round trip (zaragoza.py:38-50)."""
+    from totri_gb300.data import Zaragoza
+    m = _zaragoza_mapping()
+    ds = Zaragoza(m)
+    assert (ds.bin_def.width, ds.bin_def.offset, ds.bin_def.num) == (0.01, 0.2, 64)
+    # position (0.1, -1.0, 0.2) in the file frame is (0.1, 0.2, 1.0) on the wall
+    assert np.allclose(ds.volume_def.start, (-0.3, -0.2, 0.6))
+    assert np.allclose(ds.volume_def.end, (0.5, 0.6, 1.4))
+    assert tuple(ds.volume_def.resolution) == (64, 4, 5)
+    assert torch.allclose(ds.transient[0], torch.tensor(m["data"].sum(axis=1)))
+    assert ds.scan_points.shape == (1, 4, 5, 3)
+    assert torch.allclose(ds.scan_points[0, 1, 2], torch.tensor([0.0, -1 / 3, 0.0]), atol=1e-6)
+    assert torch.allclose(ds.scan_normals[0, 0, 0], torch.tensor([0.0, 0.0, -1.0]))
+    assert torch.allclose(ds.scan_origin, torch.tensor([[0.3, 0.5, 0.4]]))
+    r = Zaragoza(m, rectify=True)
+    assert r.scan_origin is None
+    for yy, xx in ((0, 0), (3, 4), (2, 1)):
+        d = float(((ds.scan_points[0, yy, xx] - ds.scan_origin[0]) ** 2).sum() ** 0.5)
+        k = int(2 * d / 0.01)
+        assert torch.equal(r.transient[0, :, yy, xx], torch.roll(ds.transient[0, :, yy, xx], -k))
