@@ -73,3 +73,24 @@ def test_zaragoza_mapping_layout_and_rectify():
         d = float(((ds.scan_points[0, yy, xx] - ds.scan_origin[0]) ** 2).sum() ** 0.5)
         k = int(2 * d / 0.01)
         assert torch.equal(r.transient[0, :, yy, xx], torch.roll(ds.transient[0, :, yy, xx], -k))
+
+
+def test_lindell_fk2019_arrays():
+    """LindellFk2019 (reference totri/data/lindellfk2019.py:33-57) from its two
+    arrays: per-column roll by floor(tof / 32 ps), crop, [1, T, H, W] with
+    rows and columns flipped, the fixed 512 x 512 wall grid."""
+    from totri_gb300.data import LindellFk2019
+    g = np.random.default_rng(3)
+    T, W, H = 20, 3, 4
+    meas = g.random((T, W, H)).astype(np.float32)
+    tof = g.uniform(-40, 120, (W, H)).astype(np.float32)
+    ds = LindellFk2019(meas, tof, crop=16)
+    want = np.empty_like(meas)
+    for x in range(W):
+        for y in range(H):
+            want[:, x, y] = np.roll(meas[:, x, y], -int(np.floor(tof[x, y] / 32.0)))
+    want = want[:16].transpose(0, 2, 1)[:, ::-1, ::-1][None]
+    assert ds.transient.shape == (1, 16, H, W)
+    assert np.array_equal(ds.transient.numpy(), want)
+    assert ds.scan_points.shape == (1, 512, 512, 3)
+    assert abs(ds.bin_def.width_s - 32e-12) < 1e-20
