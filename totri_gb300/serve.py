@@ -103,9 +103,11 @@ class MaskCache:
         return e
 
     def put(self, key, entry):
+        """Caches a mask whose bytes the admitting request counted in flight;
+        the caller moves them from in-flight to resident (Budget.give), so the
+        sum, and the peak taken at admission, do not change."""
         self.entries[key] = entry
         self.budget.resident += entry.nbytes
-        self.budget.peak = max(self.budget.peak, self.budget.resident + self.budget.inflight)
 
     def pin(self, key):
         self.pins[key] += 1
@@ -363,6 +365,8 @@ class Server:
             del self.queue[qi]
             slot = free[0]
             stream = self.streams[slot]
+            key = (r.mesh, r.grid) if r.kind in ("render", "grad") else None
+            new_mask = key is not None and key not in self.masks.entries
             self.budget.take(need)
             r.admitted = time.perf_counter()
             try:
@@ -371,11 +375,19 @@ class Server:
                     ev = torch.cuda.Event()
                     ev.record(stream)
             except Exception as exc:  # invalid request data: fail this request only
+                if new_mask and key in self.masks.entries:
+                    need -= self._mask_bytes(r)  # cached before the failure: now resident
                 self.budget.give(need)
-                if r.kind in ("render", "grad") and (r.mesh, r.grid) in self.masks.pins:
-                    self.masks.unpin((r.mesh, r.grid))
+                if key is not None and key in self.masks.pins:
+                    self.masks.unpin(key)
                 fut.set_exception(exc)
                 return True
+            if new_mask and key in self.masks.entries:
+                # the mask computed for this request stays cached: its bytes,
+                # counted in `need`, now belong to the resident state
+                mb = self._mask_bytes(r)
+                self.budget.give(mb)
+                need -= mb
             self.inflight[slot] = (r, fut, ev, need, result)
             return True
         return False
