@@ -44,3 +44,21 @@ def test_mask_cache_get_miss_and_pin_counts():
     assert not c.make_room(100)  # still pinned once
     c.unpin(("m", "g"))
     assert c.make_room(100)
+
+
+def test_new_mask_moves_from_inflight_to_resident():
+    """A request that computes a mask counts it in flight at admission; when
+    the mask is cached its bytes move to the resident state, so the sum, and
+    the peak, never exceed what admission checked."""
+    b = Budget(1000)
+    c = MaskCache(b)
+    b.resident = 400
+    need = 600  # outputs 400 + mask 200
+    assert b.fits(need)
+    b.take(need)
+    c.put("m", entry(200))  # cached during the launch
+    b.give(200)             # ... and handed over to the resident state
+    assert (b.resident, b.inflight, b.peak) == (600, 400, 1000)
+    assert b.resident + b.inflight <= b.total
+    b.give(need - 200)      # request done: the mask stays cached
+    assert (b.resident, b.inflight, b.free()) == (600, 0, 400)
