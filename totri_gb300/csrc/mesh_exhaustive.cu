@@ -118,8 +118,8 @@ __device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int
   return od;
 }
 
-template <int LT>
-__global__ void __launch_bounds__(256) exh_splat_kernel(Scene sc, View3f sp, View3f lp, Origins org,
+template <int LT, int kOcc = 1>
+__global__ void __launch_bounds__(256, kOcc) exh_splat_kernel(Scene sc, View3f sp, View3f lp, Origins org,
                                                         int S, int L, float* __restrict__ out,
                                                         int T, float bw, float bo, FastBins fb) {
   extern __shared__ float hist[];  // [T][LT]
@@ -442,6 +442,22 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
   // detector x 16x16 laser points) they took 4.4 s against 4.9 s for the
   // compacted variant, which "mesh.exhaustive.splat.mode" = 1 selects.
   if (tune::get("mesh.exhaustive.splat.mode") != 1) {
+    // Registers capped for 5 CTAs per SM (48, no spills): 36.5 ms against
+    // 38.1 ms uncapped (58 registers; "mesh.exhaustive.splat.occupancy" = 1)
+    // on one 20k-face mesh, 32x32 x 16x16 points, 2,048 bins.
+    if (tune::get("mesh.exhaustive.splat.occupancy") != 1) {
+      static int configured5 = 0;
+      if (smem > 48 * 1024 && configured5 < (int)smem) {
+        TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT, 5>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        configured5 = (int)smem;
+      }
+      TOTRI_KERNEL("mesh exhaustive splat", stream,
+                   (exh_splat_kernel<LT, 5><<<grid, 256, smem, stream>>>(
+                       sc, sp, lp, org, S, L, out, T, bw, bo, fast)));
+      return TOTRI_OK;
+    }
     static int configured = 0;
     if (smem > 48 * 1024 && configured < (int)smem) {
       TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT>,
