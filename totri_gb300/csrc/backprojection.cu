@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int
 // velten_confocal_kernel, so the two give identical volumes.
 constexpr int kBX = 8, kBY = 8, kBZ = 4, kST = 32, kWinRows = 256;
 
-template <int VZ>
-__global__ void __launch_bounds__(256) velten_confocal_tiled_kernel(
+template <int VZ, int kOcc = 1>
+__global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
     Grid g, int b, int T, int S, Pts3 sp, Pts3 so, int has_origin, float bw, float bo,
     FastBin fb, const float* __restrict__ tr, float* __restrict__ vol) {
   __shared__ float win[kWinRows * (kST + 1)];
@@ -490,7 +490,15 @@ int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
     const bp::FastBin fb = bp::make_fast_bin(bw, bo);
     const float* trp = static_cast<const float*>(transient->data);
     float* volp = static_cast<float*>(volume->data);
-    if (tiled && vz == 4)
+    // 4 voxels per thread with registers capped for 6 CTAs per SM (38, no
+    // spills; 34 KB of shared memory each): 38.2 ms against 40.4 ms uncapped
+    // (47 registers, 5 CTAs; "backprojection.velten.occupancy" = 1), the same
+    // volume bit for bit.
+    if (tiled && vz == 4 && tune::get("backprojection.velten.occupancy") != 1)
+      TOTRI_KERNEL("backprojection velten confocal", stream,
+                   (bp::velten_confocal_tiled_kernel<4, 6><<<grid, 256, 0, stream>>>(
+                       g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp)));
+    else if (tiled && vz == 4)
       TOTRI_KERNEL("backprojection velten confocal", stream,
                    bp::velten_confocal_tiled_kernel<4><<<grid, 256, 0, stream>>>(
                        g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp));
