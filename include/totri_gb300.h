@@ -113,7 +113,13 @@ int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t*
  * totri_mesh_workspace) fail with TOTRI_ERR_WORKSPACE before any work is
  * enqueued. All calls share that array: calls that overlap on the GPU race
  * and must be serialised by the caller. The first call on each device looks
- * up the array's device address; make it before any stream capture. */
+ * up the array's device address; make it before any stream capture, and do
+ * not call this entry point again on a device after cudaDeviceReset in the
+ * same process (the address it keeps would be stale). It reports no device
+ * status: a face index outside [0, V) ends the face list as in
+ * totri_mesh_confocal_forward, and a BVH search reaching its step limit
+ * (which a valid mesh does not reach) goes unreported; callers that need
+ * totri_mesh_workspace_status use totri_mesh_confocal_forward. */
 int totri_mesh_confocal_forward_noalloc(const totri_array_t* verts, const totri_array_t* faces,
                                         const totri_array_t* material,
                                         const totri_array_t* scan_points,

@@ -23,7 +23,9 @@ HARNESS = os.path.join(HERE, "ref_harness")
 STUBS = os.path.join(HARNESS, "stubs")
 OUT = os.path.join(HERE, "_ref")
 GEN = os.path.join(OUT, "gen")
-REF_SRC = os.path.join(os.environ.get("TOTRI_REFERENCE", "/root/reference"), "src")
+# The reference tree: $TOTRI_REFERENCE, else where this container mounts it.
+REF_ROOT = os.environ.get("TOTRI_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 LIB = os.path.join(OUT, "libref_kernels.so")
 CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 

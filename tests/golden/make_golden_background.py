@@ -14,7 +14,10 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.ref_harness import REF_ROOT  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else REF_ROOT
 
 
 def main():

@@ -1,9 +1,9 @@
 """Exhaustive (laser + detector) mesh path on the GPU against the CPU oracle and
 the reference's golden vectors.
 
-Tolerances (rel-L2): transients 1e-5 vs the FP64 oracle (masks exact);
-gradients 1e-3 vs the FP64 oracle; 1e-4 / 1e-3 vs the reference's FP32
-forward / gradient.
+Tolerances (rel-L2): transients and gradients 1e-5 vs the FP64 oracle (masks
+exact); 1e-4 / 1e-3 vs the reference's FP32 forward / gradient (its own FP32
+bin coordinates move its gradient by up to ~1e-4 from the FP64 value).
 """
 import os
 
@@ -48,8 +48,8 @@ def test_forward_and_grad_match_oracle(cuda_lib):
     rv, rm = oracle.mesh_exhaustive_grad(n["verts"], n["faces"], n["colors"], spn, lpn, None,
                                          None, vs, vl, bd.num, bd.width, bd.offset,
                                          w[0].cpu().numpy())
-    assert rel_l2(verts.grad[0].cpu().numpy(), rv) < 1e-3
-    assert rel_l2(colors.grad[0].cpu().numpy(), rm) < 1e-3
+    assert rel_l2(verts.grad[0].cpu().numpy(), rv) < 1e-5
+    assert rel_l2(colors.grad[0].cpu().numpy(), rm) < 1e-5
 
 
 def test_masks_are_the_confocal_masks(cuda_lib):

@@ -64,6 +64,8 @@ def test_noalloc_refuses_inputs_beyond_its_scratch(cuda_lib):
     colors = torch.zeros((1, 64, 0), device="cuda")
     sp = torch.zeros((1, 16384, 3), device="cuda")
     out = torch.zeros((1, 8, 16384), device="cuda")
+    # the refusal rests on this input's scratch exceeding the 24 MiB array
+    assert cuda_lib.totri_mesh_workspace(1, 64, 20480, 16384) > (24 << 20)
     st = fn(_lib.array(verts), _lib.array(faces), _lib.array(colors), _lib.array(sp),
             _lib.array(sp[:, :0]), _lib.array(out), 0.01, 0.0, 0, _lib.stream_of(out.device))
     assert st == _lib.TOTRI_ERR_WORKSPACE

@@ -542,12 +542,8 @@ int totri_backprojection_confocal_velten_adjoint(const totri_array_t* volume,
   if (numel(transient) == 0) return TOTRI_OK;
   const size_t smem = sizeof(float) * (size_t)T * bp::kTS;
   if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many bins for one tile");
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(bp::velten_adjoint_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(bp::velten_adjoint_kernel), smem));
   for (int b = 0; b < (int)B; ++b)
     TOTRI_KERNEL("backprojection velten adjoint", stream,
                  bp::velten_adjoint_kernel<<<(unsigned)ceil_div(S, bp::kTS), 256, smem, stream>>>(

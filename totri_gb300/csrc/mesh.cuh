@@ -25,8 +25,9 @@ namespace mesh {
 //           lo/hi = face AABB grown by delta: hit points must lie inside.
 // ShadeRec: (v0.xyz, albedo) (v1.xyz, vi0) (v2.xyz, vi1) (c.xyz, vi2)
 //           original vertices, FP32 centroid, vertex indices.
-// Node:     (lo0.xyz, hi0.x) (hi0.yz, lo1.xy) (lo1.z, hi1.xyz) (c0, c1, -, -)
-//           child >= 0: internal node, child < 0: leaf ~child.
+// Node:     (lo0.xy, hi0.xy) (lo1.xy, hi1.xy) (lo0.z, lo1.z, hi0.z, hi1.z) (c0, c1, -, -)
+//           child >= 0: internal node, child < 0: leaf ~child. Each pair of
+//           planes that one paired FMA evaluates (node_slabs) is adjacent.
 // Adj:      int4 (a0, a1, a2, -): a_e = Morton position of the face sharing
 //           the edge opposite vertex e (vertex indices compared), -1 if none.
 
@@ -173,6 +174,11 @@ __device__ __forceinline__ const float4* shade_at(const Scene& s, int b, int k) 
 __device__ __forceinline__ const float4* node_at(const Scene& s, int b, int i) {
   return s.nodes + ((size_t)b * s.F + i) * 4;
 }
+// Float index in a node record of child c's lower (hi = 0) or upper (hi = 1)
+// plane on axis a; the child links are floats 12 and 13.
+__host__ __device__ __forceinline__ int node_plane(int c, int hi, int a) {
+  return a < 2 ? 4 * c + 2 * hi + a : 8 + 2 * hi + c;
+}
 
 // FP32 ray-triangle test (two-sided Moller-Trumbore with t in [0, tmax] and
 // the hit point fma(t, d, o) inside the grown face AABB). Mirrors
@@ -223,6 +229,77 @@ __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, flo
 
 __device__ __forceinline__ float safe_inv(float d) {
   return fabsf(d) < 1e-20f ? copysignf(1e20f, d) : 1.f / d;
+}
+
+// Two floats in one 64-bit register pair, for the paired FP32 FMA of sm_100
+// and later (fma.rn.f32x2): each half is one correctly rounded fma, the same
+// value fmaf gives.
+__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// A ray's slab constants for node_slabs: 1/d and -o/d as (x, y) and (z, z)
+// pairs.
+struct RaySlab {
+  unsigned long long ixy, izz, nxy, nzz;
+};
+
+__device__ __forceinline__ RaySlab ray_slab(fv3 inv, fv3 oinv) {
+  return RaySlab{f2pack(inv.x, inv.y), f2pack(inv.z, inv.z), f2pack(-oinv.x, -oinv.y),
+                 f2pack(-oinv.z, -oinv.z)};
+}
+
+// The direction octant of a ray for node_slabs: bit a set when component a of
+// 1/d is negative.
+__device__ __forceinline__ int ray_octant(fv3 inv) {
+  return (signbit(inv.x) ? 1 : 0) | (signbit(inv.y) ? 2 : 0) | (signbit(inv.z) ? 4 : 0);
+}
+
+// Both children's slab tests of a node record (n0, n1, n2 as laid out in
+// Node), each against the ray segment (-inf, limit]: the twelve plane
+// distances take six paired FMAs. kOct < 8 is the ray's octant (ray_octant),
+// which fixes each axis's entry and exit plane at compile time; kOct = 8 takes
+// them with min/max. For a box with lo <= hi the two agree exactly (fma is
+// monotone), and the test accepts the boxes slab() accepts.
+template <int kOct>
+__device__ __forceinline__ void node_slabs(float4 n0, float4 n1, float4 n2, const RaySlab& r,
+                                           float limit, bool& h0, bool& h1, float& t0,
+                                           float& t1) {
+  float l0x, l0y, u0x, u0y, l1x, l1y, u1x, u1y, l0z, l1z, u0z, u1z;
+  f2unpack(f2fma(f2pack(n0.x, n0.y), r.ixy, r.nxy), l0x, l0y);
+  f2unpack(f2fma(f2pack(n0.z, n0.w), r.ixy, r.nxy), u0x, u0y);
+  f2unpack(f2fma(f2pack(n1.x, n1.y), r.ixy, r.nxy), l1x, l1y);
+  f2unpack(f2fma(f2pack(n1.z, n1.w), r.ixy, r.nxy), u1x, u1y);
+  f2unpack(f2fma(f2pack(n2.x, n2.y), r.izz, r.nzz), l0z, l1z);
+  f2unpack(f2fma(f2pack(n2.z, n2.w), r.izz, r.nzz), u0z, u1z);
+  float a0, b0, a1, b1;  // entry / exit distance of each child
+  if (kOct == 8) {
+    a0 = fmax3(fminf(l0x, u0x), fminf(l0y, u0y), fminf(l0z, u0z));
+    b0 = fmin3(fmaxf(l0x, u0x), fmaxf(l0y, u0y), fminf(fmaxf(l0z, u0z), limit));
+    a1 = fmax3(fminf(l1x, u1x), fminf(l1y, u1y), fminf(l1z, u1z));
+    b1 = fmin3(fmaxf(l1x, u1x), fmaxf(l1y, u1y), fminf(fmaxf(l1z, u1z), limit));
+  } else {
+    constexpr bool nx = kOct & 1, ny = kOct & 2, nz = kOct & 4;
+    a0 = fmax3(nx ? u0x : l0x, ny ? u0y : l0y, nz ? u0z : l0z);
+    b0 = fmin3(nx ? l0x : u0x, ny ? l0y : u0y, fminf(nz ? l0z : u0z, limit));
+    a1 = fmax3(nx ? u1x : l1x, ny ? u1y : l1y, nz ? u1z : l1z);
+    b1 = fmin3(nx ? l1x : u1x, ny ? l1y : u1y, fminf(nz ? l1z : u1z, limit));
+  }
+  h0 = a0 <= b0;
+  h1 = a1 <= b1;
+  t0 = a0;
+  t1 = a1;
 }
 
 // The target of a visibility query: face k (Morton position) with its
@@ -298,8 +375,8 @@ __device__ bool target_visible(const Scene& sc, int b, int n, const Target& tg, 
     const float4* nd = node_at(sc, b, node);
     const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
     float tn0, tn1;
-    bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
-    bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+    bool h0 = slab(n0.x, n0.y, n2.x, n0.z, n0.w, n2.z, inv, oinv, tf, tn0);
+    bool h1 = slab(n1.x, n1.y, n2.y, n1.z, n1.w, n2.w, inv, oinv, tf, tn1);
     const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
     if (h0 && c0 < 0) {
       if (occludes(~c0)) { cache = ~c0; return false; }
@@ -432,15 +509,13 @@ __device__ __forceinline__ int query_prefix(const Scene& sc, int b, int n, const
   return 1;
 }
 
-// The BVH search of target_visible_pp: true when some face other than the
-// target k (original index f) hits the ray before the target's hit at tf
-// (ties to the lower original index); `seed` returns that occluder.
-__device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int k, int f, fv3 o,
-                                             fv3 dir, float tmax, float tf, uint32_t* status,
-                                             int& seed) {
+// The BVH search of target_visible_pp for rays of octant kOct (node_slabs).
+template <int kOct>
+__device__ __forceinline__ bool bvh_occluded_oct(const Scene& sc, int b, int n, int k, int f,
+                                                 fv3 o, fv3 dir, float tmax, float tf,
+                                                 const RaySlab& rs, uint32_t* status,
+                                                 int& seed) {
   constexpr int kDone = INT_MIN;  // below every leaf code ~k, k < n
-  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
-  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   int stack[64];
   int sp = 0;
   auto pop = [&]() { return sp > 0 ? stack[--sp] : kDone; };
@@ -458,8 +533,8 @@ __device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int 
       const float4* nd = nodes + node * 4;
       const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
       float tn0, tn1;
-      const bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
-      const bool h1 = slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+      bool h0, h1;
+      node_slabs<kOct>(n0, n1, n2, rs, tf, h0, h1, tn0, tn1);
       const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
       if (h0 && h1) {
         const bool first0 = tn0 <= tn1;
@@ -503,6 +578,32 @@ __device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int 
     }
   }
   return false;
+}
+
+// The BVH search of target_visible_pp: true when some face other than the
+// target k (original index f) hits the ray before the target's hit at tf
+// (ties to the lower original index); `seed` returns that occluder. When the
+// rays of all calling lanes share a direction octant with d.z >= 0 (rays
+// from a wall patch towards one face mostly do), the walk with that octant's
+// fixed entry and exit planes runs; otherwise the general one. Every lane of
+// the warp that calls it takes the same branch.
+__device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int k, int f, fv3 o,
+                                             fv3 dir, float tmax, float tf, uint32_t* status,
+                                             int& seed) {
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const RaySlab rs = ray_slab(inv, oinv);
+  const unsigned act = __activemask();
+  const int oct = ray_octant(inv);
+  const int lead = __shfl_sync(act, oct, __ffs(act) - 1);
+  const int mode = __all_sync(act, oct == lead) && lead < 4 ? lead : 8;
+  switch (mode) {
+    case 0: return bvh_occluded_oct<0>(sc, b, n, k, f, o, dir, tmax, tf, rs, status, seed);
+    case 1: return bvh_occluded_oct<1>(sc, b, n, k, f, o, dir, tmax, tf, rs, status, seed);
+    case 2: return bvh_occluded_oct<2>(sc, b, n, k, f, o, dir, tmax, tf, rs, status, seed);
+    case 3: return bvh_occluded_oct<3>(sc, b, n, k, f, o, dir, tmax, tf, rs, status, seed);
+    default: return bvh_occluded_oct<8>(sc, b, n, k, f, o, dir, tmax, tf, rs, status, seed);
+  }
 }
 
 __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
@@ -601,8 +702,8 @@ __device__ __forceinline__ int shaft_candidates(const Scene& sc, int b, int n, i
           const float4* nd = nodes + node * 4;
           const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2),
                        n3 = __ldg(nd + 3);
-          h0 = shaft_box(h, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-          h1 = shaft_box(h, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+          h0 = shaft_box(h, n0.x, n0.y, n2.x, n0.z, n0.w, n2.z);
+          h1 = shaft_box(h, n1.x, n1.y, n2.y, n1.z, n1.w, n2.w);
           c0 = __float_as_int(n3.x);
           c1 = __float_as_int(n3.y);
         } else {
@@ -793,8 +894,8 @@ __device__ __forceinline__ bool packet_visible(const Scene& sc, int b, int n, bo
     const float4* nd = node_at(sc, b, node);
     const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
     float tn0 = 0.f, tn1 = 0.f;
-    bool h0 = active && slab(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oinv, tf, tn0);
-    bool h1 = active && slab(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oinv, tf, tn1);
+    bool h0 = active && slab(n0.x, n0.y, n2.x, n0.z, n0.w, n2.z, inv, oinv, tf, tn0);
+    bool h1 = active && slab(n1.x, n1.y, n2.y, n1.z, n1.w, n2.w, inv, oinv, tf, tn1);
     const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
     if (c0 < 0) {
       if (h0 && occludes(~c0)) active = vis = false;

@@ -13,6 +13,7 @@
 //   7. hierarchy Karras 2012 internal nodes, parent links
 //   8. refit     bottom-up boxes (second arrival at a node merges its children)
 #include "mesh.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace mesh {
@@ -399,16 +400,18 @@ __global__ void refit_kernel(Scene sc) {
   while (node >= 0) {
     float* nd = reinterpret_cast<float*>(sc.nodes + (base + node) * 4);
     const int c0 = __float_as_int(nd[12]);
-    float* slot = nd + (c0 == child ? 0 : 6);
-    slot[0] = lo[0]; slot[1] = lo[1]; slot[2] = lo[2];
-    slot[3] = hi[0]; slot[4] = hi[1]; slot[5] = hi[2];
+    const int side = c0 == child ? 0 : 1;
+    for (int a = 0; a < 3; ++a) {
+      nd[node_plane(side, 0, a)] = lo[a];
+      nd[node_plane(side, 1, a)] = hi[a];
+    }
     __threadfence();
     if (atomicAdd(&sc.counter[base + node], 1) == 0) return;
     __threadfence();
     const volatile float* vn = nd;
     for (int a = 0; a < 3; ++a) {
-      lo[a] = fminf(vn[a], vn[6 + a]);
-      hi[a] = fmaxf(vn[3 + a], vn[9 + a]);
+      lo[a] = fminf(vn[node_plane(0, 0, a)], vn[node_plane(1, 0, a)]);
+      hi[a] = fmaxf(vn[node_plane(0, 1, a)], vn[node_plane(1, 1, a)]);
     }
     child = node;
     node = sc.iparent[base + node];
@@ -439,12 +442,12 @@ __global__ void widen_kernel(Scene sc) {
   for (int side = 0; side < 2; ++side) {
     const int c = __float_as_int(nd[12 + side]);
     if (c < 0 || c >= n - 1) {  // leaf (or malformed link: walked and flagged later)
-      for (int a = 0; a < 6; ++a) box[a][m] = nd[6 * side + a];
+      for (int a = 0; a < 6; ++a) box[a][m] = nd[node_plane(side, a / 3, a % 3)];
       code[m++] = c;
     } else {
       const float* cn = reinterpret_cast<const float*>(sc.nodes + (base + c) * 4);
       for (int g = 0; g < 2; ++g) {
-        for (int a = 0; a < 6; ++a) box[a][m] = cn[6 * g + a];
+        for (int a = 0; a < 6; ++a) box[a][m] = cn[node_plane(g, a / 3, a % 3)];
         code[m++] = __float_as_int(cn[12 + g]);
       }
     }
@@ -536,12 +539,8 @@ __global__ void edge_link_kernel(Scene sc) {
 
 int launch_point_order(const Scene& sc, const View3f& pts, int P, cudaStream_t stream) {
   const size_t smem = sizeof(uint32_t) * (32 * kSortDigits + 2 * kSortDigits);
-  static bool attr_set = false;
-  if (!attr_set) {
-    TOTRI_CUDA(cudaFuncSetAttribute(point_order_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(point_order_kernel), smem));
   TOTRI_KERNEL("mesh point order", stream,
                point_order_kernel<<<sc.B, kSortThreads, smem, stream>>>(pts, P, sc.B,
                                                                          sc.pscratch));
@@ -559,12 +558,8 @@ int build_scene(const Scene& sc, const BuildInputs& in, cudaStream_t stream) {
     TOTRI_KERNEL("mesh bounds", stream, bounds_kernel<<<gridF, blk, 0, stream>>>(sc, in));
     TOTRI_KERNEL("mesh morton", stream, morton_kernel<<<gridF, blk, 0, stream>>>(sc, in));
     const size_t smem = sizeof(uint32_t) * (32 * kSortDigits + 2 * kSortDigits);
-    static bool attr_set = false;
-    if (!attr_set) {
-      TOTRI_CUDA(cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-      attr_set = true;
-    }
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(sort_kernel), smem));
     TOTRI_KERNEL("mesh sort", stream, sort_kernel<<<B, kSortThreads, smem, stream>>>(sc));
     TOTRI_KERNEL("mesh records", stream, records_kernel<<<gridF, blk, 0, stream>>>(sc, in));
     TOTRI_CUDA(cudaMemsetAsync(sc.ekeys, 0xff, sizeof(unsigned long long) * B * sc.ecap, stream));

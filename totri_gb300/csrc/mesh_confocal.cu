@@ -242,6 +242,126 @@ __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, V
   }
 }
 
+// visibility_patch_kernel<0> with the BVH searches compacted. After a face's
+// prefix (the target's own hit and, for faces seen from behind, the surface
+// walk) only some lanes are still undecided: most hidden targets are settled
+// by the walk, so a face seen from behind typically leaves a few rays, and
+// the warp used to run their BVH walks with the other lanes idle. Here each
+// undecided ray goes into its warp's queue in shared memory (its direction,
+// limits and target), and the warp walks the BVH only for full batches of 32
+// queued rays, one per lane, drawn from the faces it has taken so far (and the
+// last partial batch at the end). A face's mask word is written when its
+// prefix ends, with the queued rays counted visible, and a walk that finds an
+// occluder clears its bit. The decisions per ray are those of
+// target_visible_pp (same prefix, same search), so the masks are unchanged.
+constexpr int kVisQueue = 64;  // entries per warp: < 32 left over + 32 added
+
+template <int kOcc>
+__global__ void __launch_bounds__(256, kOcc) visibility_queue_kernel(Scene sc, View3f pts, int P,
+                                                                    int row0, int chunks,
+                                                                    int seed_mode,
+                                                                    int seed_steps) {
+  __shared__ uint32_t bits[kMaxPatchChunks][32];
+  __shared__ int seeds[32];
+  __shared__ int next_face;
+  __shared__ float opts[3][32];  // the block's wall points (ray origins)
+  // per warp: (dir.xyz, tf) and (tmax, target k << 5 | point lane, face index, -)
+  __shared__ float4 queue[8][kVisQueue][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = blockIdx.z;
+  const int ch0 = blockIdx.y * chunks;
+  const int i = blockIdx.x * 32 + lane;  // position in Morton order
+  const int n = sc.meta[b].n;
+  const bool okp = i < P;
+  const uint32_t* order = sc.pscratch + 3 * (size_t)sc.B * P + (size_t)b * P;
+  const int p = okp ? (int)order[i] : 0;
+  const fv3 o = okp ? mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2)) : mkv(0.f, 0.f, 0.f);
+  volatile int* vseeds = seeds;
+  volatile int* gseeds = reinterpret_cast<int*>(sc.pscratch) + (size_t)b * P;
+  if (threadIdx.x < 32) {
+    seeds[lane] = okp ? gseeds[i] : -1;
+    opts[0][lane] = o.x;
+    opts[1][lane] = o.y;
+    opts[2][lane] = o.z;
+  }
+  if (threadIdx.x == 0) next_face = 0;
+  __syncthreads();
+  const int nc = min(chunks, sc.nch - ch0);
+  const uint32_t below = (1u << lane) - 1u;
+  float4(*q)[2] = queue[warp];
+  int cnt = 0;  // queued rays (warp-uniform)
+  // Walks queue entries [0, m), entry `lane` on lane `lane`.
+  auto walk = [&](int m) {
+    if (lane < m) {
+      const float4 a = q[lane][0], e = q[lane][1];
+      const int code = __float_as_int(e.y);
+      const int k = code >> 5, pl = code & 31;
+      const fv3 oo = mkv(opts[0][pl], opts[1][pl], opts[2][pl]);
+      int seed = -1;
+      if (bvh_occluded(sc, b, n, k, __float_as_int(e.z), oo, mkv(a.x, a.y, a.z), e.x, a.w,
+                       sc.status, seed)) {
+        const int t = k - ch0 * 32;
+        atomicAnd(&bits[t >> 5][t & 31], ~(1u << pl));
+        vseeds[pl] = seed;
+      }
+    }
+  };
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(&next_face, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= nc * 32) break;
+    const int c = t >> 5, j = t & 31;
+    const int k = (ch0 + c) * 32 + j;
+    if (k >= n) {  // warp-uniform
+      if (lane == 0) bits[c][j] = 0u;
+      continue;
+    }
+    bool vis = false;
+    int need = 0;
+    const Target tg = load_target(sc, b, k);
+    fv3 dir = mkv(0.f, 0.f, 0.f);
+    float tmax = 0.f, tf = 0.f;
+    if (okp) {
+      const int s0 = vseeds[lane];
+      int seed = s0;
+      need = query_prefix(sc, b, n, tg, o, seed, seed_mode, seed_steps, dir, tmax, tf, vis);
+      if (seed != s0) vseeds[lane] = seed;
+    }
+    const uint32_t nm = __ballot_sync(0xffffffffu, need);
+    const uint32_t w = __ballot_sync(0xffffffffu, vis || need);
+    if (lane == 0) bits[c][j] = w;
+    if (need) {
+      const int at = cnt + __popc(nm & below);
+      q[at][0] = make_float4(dir.x, dir.y, dir.z, tf);
+      q[at][1] = make_float4(tmax, __int_as_float((k << 5) | lane), __int_as_float(tg.f), 0.f);
+    }
+    cnt += __popc(nm);
+    if (cnt >= 32) {
+      __syncwarp();
+      walk(32);
+      __syncwarp();
+      if (lane < cnt - 32) {
+        q[lane][0] = q[32 + lane][0];
+        q[lane][1] = q[32 + lane][1];
+      }
+      cnt -= 32;
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+  walk(cnt);
+  __syncthreads();
+  if (threadIdx.x < 32 && okp) gseeds[i] = seeds[lane];
+  for (int c = warp; c < nc; c += 8) {
+    if (!okp) continue;
+    uint32_t word = 0u;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) word |= ((bits[c][j] >> lane) & 1u) << j;
+    sc.mask[((size_t)b * sc.P + row0 + p) * sc.nch + ch0 + c] = word;
+  }
+}
+
 // Per-pair confocal geometry: FP32 decisions exactly as the oracle takes them.
 struct ConfocalPair {
   fv3 v[3];
@@ -438,13 +558,27 @@ __global__ void __launch_bounds__(256, 2) splat_compact_kernel(Scene sc, View3f 
   flush_tile<TS>(hist, transient + (size_t)b * T * S, T, S, s0);
 }
 
+// The tent corners of a pair relative to its first bin, from double-float
+// path lengths 2 |v_k - p| + od (bin_offset); od is the double-float origin
+// term 2 |p - o| (zero without origins).
+__device__ __forceinline__ void confocal_corners(const ConfocalPair& q, fv3 p, DFloat od, float bw,
+                                                 float inv_bw, float bo, float x[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const DFloat d = len_df(q.v[k], p);
+    x[k] = bin_offset(df_add(DFloat{2.f * d.hi, 2.f * d.lo}, od), bo, bw, inv_bw, q.bin[0]);
+  }
+}
+
 // Gradient of one visible pair with respect to the three (sorted) vertices and
 // the albedo, following mesh_confocal_grad_verts_optix.cu:248-314 and
-// AlphaConfocalGradVerts (mesh_common.h:429-463). Returns false when the pair
+// AlphaConfocalGradVerts (mesh_common.h:429-463), with the tent corners x taken
+// relative to bin[0] (confocal_corners). Returns false when the pair
 // contributes nothing.
-__device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c, fv3 p, float rho,
-                                                   float bw, const float* __restrict__ tg_col,
-                                                   int T, int S, fv3 dv[3], float& dmat) {
+__device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, const float x[3], fv3 c,
+                                                   fv3 p, float rho, float bw,
+                                                   const float* __restrict__ tg_col, int T, int S,
+                                                   fv3 dv[3], float& dmat) {
   const float alpha = alpha_confocal(q, c, p, rho);
   if (!(alpha > 0.f)) return false;
   if (q.bin[0] >= T || q.bin[2] < 0) return false;
@@ -472,9 +606,9 @@ __device__ __forceinline__ bool pair_grad_confocal(const ConfocalPair& q, fv3 c,
     return true;
   }
   TentGrad tgr;
-  tent_grad(tg_col, S, T, q.c, q.bin, tgr);
+  tent_grad(tg_col, S, T, x, q.bin, tgr);
   // part1 = Ayc * dyc + A0 * dc0 + A1 * dc1 + A2 * dc2 (see TentGrad)
-  const float span = q.c[2] - q.c[0];
+  const float span = x[2] - x[0];
   const float kk = vdiv(-4.f, bw * span * span);
   const fv3 r0 = q.v[0] - p, r1 = q.v[1] - p, r2 = q.v[2] - p;
   const fv3 dc0 = vdiv(2.f, bw * q.d[0]) * r0;
@@ -512,6 +646,7 @@ __global__ void __launch_bounds__(256, 3) grad_kernel(Scene sc, View3f sp, View3
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const float* tgb = tgrad + (size_t)b * T * S;
   const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  const float inv_bw = __frcp_rn(bw);
   for (int j = warp; j < 32; j += nw) {
     const int k = ch * 32 + j;
     if (k >= n) break;
@@ -523,13 +658,21 @@ __global__ void __launch_bounds__(256, 3) grad_kernel(Scene sc, View3f sp, View3
     auto run = [&](int s) {
       const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
       float od = 0.f;
-      if (has_origin)
-        od = xmul(2.f, xlen(xsub3(p, mkv(so.at(b, s, 0), so.at(b, s, 1), so.at(b, s, 2)))));
+      DFloat odf{0.f, 0.f};
+      if (has_origin) {
+        const fv3 o = mkv(so.at(b, s, 0), so.at(b, s, 1), so.at(b, s, 2));
+        od = xmul(2.f, xlen(xsub3(p, o)));
+        const DFloat d = len_df(p, o);
+        odf = DFloat{2.f * d.hi, 2.f * d.lo};
+      }
       ConfocalPair q;
       confocal_pair(s0r, s1r, s2r, p, od, bw, bo, q);
+      if (q.bin[0] >= T || q.bin[2] < 0) return;
+      float x[3];
+      confocal_corners(q, p, odf, bw, inv_bw, bo, x);
       fv3 dv[3];
       float dm;
-      if (!pair_grad_confocal(q, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) return;
+      if (!pair_grad_confocal(q, x, c, p, s0r.w, bw, tgb + s, T, S, dv, dm)) return;
       add_permuted(acc, dv, q.perm);
       accm += dm;
     };
@@ -636,12 +779,29 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
       TOTRI_KERNEL("mesh visibility", stream,
                    visibility_patch_kernel<3><<<grid, 256, 0, stream>>>(
                        sc, pts, P, row0, chunks, seed_mode, seed_steps, shaft_cap));
+    // The queued BVH searches (visibility_queue_kernel) when
+    // "mesh.visibility.queue" = 1; queue entries pack the target's Morton
+    // position in 26 bits.
+    else if (tune::get("mesh.visibility.queue") == 1 && sc.F < (1 << 26)) {
+      if (tune::get("mesh.visibility.occupancy") == 4)
+        TOTRI_KERNEL("mesh visibility", stream,
+                     visibility_queue_kernel<4><<<grid, 256, 0, stream>>>(
+                         sc, pts, P, row0, chunks, seed_mode, seed_steps));
+      else
+        TOTRI_KERNEL("mesh visibility", stream,
+                     visibility_queue_kernel<5><<<grid, 256, 0, stream>>>(
+                         sc, pts, P, row0, chunks, seed_mode, seed_steps));
+    }
     // Registers capped for 5 CTAs per SM (48 a thread, 28 bytes of spills):
     // 8.84 ms against 9.33 ms uncapped (60 registers, 4 CTAs) and 9.03 ms at
     // 6 CTAs (40 registers) inside the differentiable 20,480-face step.
     else if (tune::get("mesh.visibility.occupancy") == 1)
       TOTRI_KERNEL("mesh visibility", stream,
                    visibility_patch_kernel<0, 1><<<grid, 256, 0, stream>>>(
+                       sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
+    else if (tune::get("mesh.visibility.occupancy") == 4)
+      TOTRI_KERNEL("mesh visibility", stream,
+                   visibility_patch_kernel<0, 4><<<grid, 256, 0, stream>>>(
                        sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
     else if (tune::get("mesh.visibility.occupancy") == 6)
       TOTRI_KERNEL("mesh visibility", stream,
@@ -662,24 +822,16 @@ static int launch_splat_ts(const Scene& sc, const View3f& sp, const View3f& so, 
   const size_t smem = sizeof(float) * (size_t)T * TS;
   const dim3 grid((unsigned)ceil_div(S, TS), (unsigned)sc.B);
   if (tune::get("mesh.confocal.splat.mode") == 1) {
-    static int configured_c = 0;
-    if (smem > 40 * 1024 && configured_c < (int)smem) {  // 2.3 KB static shared memory besides
-      TOTRI_CUDA(cudaFuncSetAttribute(splat_compact_kernel<TS>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured_c = (int)smem;
-    }
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(splat_compact_kernel<TS>), smem));
     TOTRI_KERNEL("mesh confocal splat", stream,
                  splat_compact_kernel<TS><<<grid, 256, smem, stream>>>(
                      sc, sp, so, has_origin, transient, T, S, bw, bo,
                      make_fast_bins(bw, bo, tune::get("mesh.confocal.exact") != 1)));
     return TOTRI_OK;
   }
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(splat_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(splat_kernel<TS>), smem));
   TOTRI_KERNEL("mesh confocal splat", stream,
                splat_kernel<TS><<<grid, 256, smem, stream>>>(
                    sc, sp, so, has_origin, transient, T, S, bw, bo,
@@ -725,12 +877,8 @@ int launch_confocal_grad(const Scene& sc, const View3f& sp, const View3f& so, in
   const int split =
       tune::grad_split("mesh.confocal.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
   const size_t smem = sizeof(uint32_t) * (size_t)ceil_div(S, split);
-  static int configured = 0;
-  if (smem > 40 * 1024 && configured < (int)smem) {  // 2 KB of static shared memory besides
-    TOTRI_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(grad_kernel), smem));
   const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
   TOTRI_KERNEL("mesh confocal grad", stream,
                grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, so, has_origin, tgrad, T, S, bw,

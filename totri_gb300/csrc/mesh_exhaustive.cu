@@ -244,12 +244,35 @@ __global__ void __launch_bounds__(256) exh_splat_compact_kernel(Scene sc, View3f
   }
 }
 
+// The origin terms |s - o_s| + |l - o_l| as a double-float (zero without origins).
+__device__ __forceinline__ DFloat origin_term_df(const Origins& o, int b, int s, int l, fv3 sp,
+                                                 fv3 lp) {
+  DFloat od{0.f, 0.f};
+  if (o.has_so) od = len_df(sp, mkv(o.so.at(b, s, 0), o.so.at(b, s, 1), o.so.at(b, s, 2)));
+  if (o.has_lo)
+    od = df_add(od, len_df(lp, mkv(o.lo.at(b, l, 0), o.lo.at(b, l, 1), o.lo.at(b, l, 2))));
+  return od;
+}
+
+// The tent corners of a triple relative to its first bin, from double-float
+// path lengths |v_k - s| + |v_k - l| + od (bin_offset).
+__device__ __forceinline__ void exh_corners(const ExhPair& q, fv3 sp, fv3 lp, DFloat od, float bw,
+                                            float inv_bw, float bo, float x[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const DFloat d = df_add(df_add(len_df(q.v[k], sp), len_df(q.v[k], lp)), od);
+    x[k] = bin_offset(d, bo, bw, inv_bw, q.bin[0]);
+  }
+}
+
 // Gradient of one visible triple w.r.t. the sorted vertices and the albedo
 // (mesh_exhaustive_grad_verts_optix.cu:336-412, AlphaExhaustiveGradVerts
-// mesh_common.h:549-630).
-__device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3 lp, float rho,
-                                            float bw, const float* __restrict__ col,
-                                            int64_t stride, int T, fv3 dv[3], float& dmat) {
+// mesh_common.h:549-630), with the tent corners x taken relative to bin[0]
+// (exh_corners).
+__device__ __forceinline__ bool triple_grad(const ExhPair& q, const float x[3], fv3 c, fv3 sp,
+                                            fv3 lp, float rho, float bw,
+                                            const float* __restrict__ col, int64_t stride, int T,
+                                            fv3 dv[3], float& dmat) {
   const float alpha = alpha_exhaustive(q, c, sp, lp, rho);
   if (!(alpha > 0.f)) return false;
   if (q.bin[0] >= T || q.bin[2] < 0) return false;
@@ -276,8 +299,8 @@ __device__ __forceinline__ bool triple_grad(const ExhPair& q, fv3 c, fv3 sp, fv3
     return true;
   }
   TentGrad tgr;
-  tent_grad(col, stride, T, q.c, q.bin, tgr);
-  const float span = q.c[2] - q.c[0];
+  tent_grad(col, stride, T, x, q.bin, tgr);
+  const float span = x[2] - x[0];
   const float kk = vdiv(-2.f, bw * span * span);
   fv3 dc[3];
   for (int k = 0; k < 3; ++k)
@@ -327,9 +350,12 @@ __global__ void __launch_bounds__(256) exh_grad_kernel(Scene sc, View3f sp, View
         ExhPair e;
         exh_pair_filtered(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, fb,
                           e);
+        if (e.bin[0] >= T || e.bin[2] < 0) continue;
+        float x[3];
+        exh_corners(e, p, q, origin_term_df(org, b, s, l, p, q), bw, fb.inv_bw, bo, x);
         fv3 dv[3];
         float dm;
-        if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
+        if (!triple_grad(e, x, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
           continue;
         add_permuted(acc, dv, e.perm);
         accm += dm;
@@ -390,9 +416,12 @@ __global__ void __launch_bounds__(256) exh_grad_compact_kernel(
       ExhPair e;
       exh_pair_filtered(s0r, s1r, s2r, p, q, origin_term(org, b, s, l, p, q), bw, bo, fb,
                           e);
+      if (e.bin[0] >= T || e.bin[2] < 0) return;
+      float x[3];
+      exh_corners(e, p, q, origin_term_df(org, b, s, l, p, q), bw, fb.inv_bw, bo, x);
       fv3 dv[3];
       float dm;
-      if (!triple_grad(e, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
+      if (!triple_grad(e, x, c, p, q, s0r.w, bw, tgb + (size_t)s * L + l, stride, T, dv, dm))
         return;
       add_permuted(acc, dv, e.perm);
       accm += dm;
@@ -446,35 +475,22 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
     // 38.1 ms uncapped (58 registers; "mesh.exhaustive.splat.occupancy" = 1)
     // on one 20k-face mesh, 32x32 x 16x16 points, 2,048 bins.
     if (tune::get("mesh.exhaustive.splat.occupancy") != 1) {
-      static int configured5 = 0;
-      if (smem > 48 * 1024 && configured5 < (int)smem) {
-        TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT, 5>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-        configured5 = (int)smem;
-      }
+      TOTRI_CUDA(tune::ensure_dynamic_smem(
+          reinterpret_cast<const void*>(exh_splat_kernel<LT, 5>), smem));
       TOTRI_KERNEL("mesh exhaustive splat", stream,
                    (exh_splat_kernel<LT, 5><<<grid, 256, smem, stream>>>(
                        sc, sp, lp, org, S, L, out, T, bw, bo, fast)));
       return TOTRI_OK;
     }
-    static int configured = 0;
-    if (smem > 48 * 1024 && configured < (int)smem) {
-      TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_kernel<LT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured = (int)smem;
-    }
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(exh_splat_kernel<LT>), smem));
     TOTRI_KERNEL("mesh exhaustive splat", stream,
                  exh_splat_kernel<LT><<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, out, T,
                                                                    bw, bo, fast));
     return TOTRI_OK;
   }
-  static int configured = 0;
-  if (smem > 32 * 1024 && configured < (int)smem) {  // 16 KB of static shared memory besides
-    TOTRI_CUDA(cudaFuncSetAttribute(exh_splat_compact_kernel<LT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(exh_splat_compact_kernel<LT>), smem));
   TOTRI_KERNEL("mesh exhaustive splat", stream,
                exh_splat_compact_kernel<LT><<<grid, 256, smem, stream>>>(
                    sc, sp, lp, org, S, L, out, T, bw, bo, fast));
@@ -533,12 +549,8 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
     const size_t smem = sizeof(uint32_t) * (size_t)(S + L);
     if (smem > 200 * 1024)
       return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points for one tile");
-    static int configured = 0;
-    if (smem > 48 * 1024 && configured < (int)smem) {
-      TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      configured = (int)smem;
-    }
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(exh_grad_kernel), smem));
     const dim3 grid((unsigned)sc.nch, (unsigned)sc.B, (unsigned)split);
     TOTRI_KERNEL("mesh exhaustive grad", stream,
                  exh_grad_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T,
@@ -547,12 +559,8 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   }
   const size_t smem = sizeof(uint32_t) * (size_t)(slice + 32 * ceil_div(L, 32));
   if (smem > 180 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many laser points for one tile");
-  static int configured = 0;
-  if (smem > 32 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(exh_grad_compact_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(exh_grad_compact_kernel), smem));
   // (three CTAs per SM at 80 registers spills and runs 6% slower: 93.5 ms
   // against 87.8 ms on one 20k-face mesh; CTAs of 5 or 6 warps capped at 96
   // registers for 4 or 3 CTAs per SM spill and took 98 and 95 ms against

@@ -101,6 +101,66 @@ __device__ __forceinline__ void flush_tile(const float* hist, float* __restrict_
   }
 }
 
+// Bin-relative tent corners for the gradients. A bin coordinate c is some
+// hundreds of bins, so its FP32 value is off by up to ~3e-5 bin; the gradient
+// weighs each bin's incoming gradient by where the tent's corners sit inside
+// the bins, and that offset alone moved the FP32 vertex gradient 1.8e-4
+// (rel-L2) from its FP64 value on the 20,480-face scene (the reference's FP32
+// kernels carry the same error). The gradient kernels therefore take the
+// corners as x = c - bin[0], from path lengths carried as unevaluated sums
+// hi + lo of two floats (double-float arithmetic: Knuth's two-sum and the
+// fused-multiply-add product error, Dekker 1971), which leaves ~1e-7 bin of
+// error; the integer bins stay those of the FP32 decisions.
+struct DFloat {
+  float hi, lo;
+};
+
+// hi + lo == a + b exactly, hi = fl(a + b) (Knuth's branch-free two-sum).
+__device__ __forceinline__ DFloat two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return DFloat{s, e};
+}
+
+// |v - p| as hi + lo, relative error near 2^-44: the coordinate differences
+// and their squares are split exactly, the sum of squares keeps its rounding
+// errors, and the square root takes one Newton correction.
+__device__ __forceinline__ DFloat len_df(fv3 v, fv3 p) {
+  const DFloat dx = two_sum(v.x, -p.x), dy = two_sum(v.y, -p.y), dz = two_sum(v.z, -p.z);
+  const float hx = __fmul_rn(dx.hi, dx.hi), hy = __fmul_rn(dy.hi, dy.hi);
+  const float hz = __fmul_rn(dz.hi, dz.hi);
+  const float lx = __fmaf_rn(dx.hi, dx.hi, -hx), ly = __fmaf_rn(dy.hi, dy.hi, -hy);
+  const float lz = __fmaf_rn(dz.hi, dz.hi, -hz);
+  const DFloat s1 = two_sum(hx, hy);
+  const DFloat s2 = two_sum(s1.hi, hz);
+  const float lo = (s1.lo + s2.lo) + (lx + ly + lz) +
+                   2.f * (dx.hi * dx.lo + dy.hi * dy.lo + dz.hi * dz.lo);
+  if (!(s2.hi > 0.f)) return DFloat{0.f, 0.f};
+  const float rs = rsqrtf(s2.hi);
+  const float r = s2.hi * rs;
+  const float res = __fmaf_rn(-r, r, s2.hi) + lo;
+  return DFloat{r, res * 0.5f * rs};
+}
+
+// a + b for double-float operands (the low parts are added, not renormalised:
+// the result feeds bin_offset only).
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+  const DFloat s = two_sum(a.hi, b.hi);
+  return DFloat{s.hi, s.lo + a.lo + b.lo};
+}
+
+// (path - bo) / bw - bin0 for a double-float path length: the quotient's
+// remainder comes from one fused multiply-add, and q - bin0 is exact because
+// bin0 is the truncated FP32 quotient of the same path.
+__device__ __forceinline__ float bin_offset(DFloat path, float bo, float bw, float inv_bw,
+                                            int bin0) {
+  const DFloat a = two_sum(path.hi, -bo);
+  const float q = a.hi * inv_bw;
+  const float rem = __fmaf_rn(-q, bw, a.hi) + (a.lo + path.lo);
+  return (q - (float)bin0) + rem * inv_bw;
+}
+
 // Gradient of the normalised tent (area 1, yc = 2 / (c2 - c0)) against the
 // incoming transient gradient g(bin) = col[bin * stride]:
 //   part0 = sum_bins g * area_bin
@@ -115,13 +175,16 @@ struct SegSums {
   float ya, yb, ca, cb;
 };
 
+// Corners and bins are relative to bin boff (x = c - boff, b = bin - boff):
+// bin b reads col[(b + boff) * stride] and exists for 0 <= b + boff < T.
 __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int64_t stride, int T,
-                                             float& part0, SegSums& sm, float ca, int ba, float ya,
-                                             float cb, int bb, float yb) {
-  auto in = [&](int b) { return b >= 0 && b < T; };
+                                             int boff, float& part0, SegSums& sm, float ca, int ba,
+                                             float ya, float cb, int bb, float yb) {
+  auto in = [&](int b) { return (unsigned)(b + boff) < (unsigned)T; };
+  auto at = [&](int b) { return __ldg(col + (int64_t)(b + boff) * stride); };
   if (ba == bb) {
     if (in(ba)) {
-      const float g = __ldg(col + ba * stride);
+      const float g = at(ba);
       const float half_span = 0.5f * (cb - ca), half_y = 0.5f * (ya + yb);
       part0 += g * half_span * (ya + yb);
       sm.ya += g * half_span;
@@ -135,7 +198,7 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
   const float slope = (yb - ya) * inv;
   const float q = slope * inv;
   if (in(ba)) {
-    const float g = __ldg(col + ba * stride);
+    const float g = at(ba);
     const float base = (float)(ba + 1) - ca;
     const float hb2 = 0.5f * base * base;
     part0 += g * base * (ya + 0.5f * base * slope);
@@ -145,9 +208,9 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
     sm.cb -= g * hb2 * q;
   }
   float sg = 0.f, sgm = 0.f;
-  const int lo = max(ba + 1, 0), hi = min(bb, T);
+  const int lo = max(ba + 1, -boff), hi = min(bb, T - boff);
   for (int i = lo; i < hi; ++i) {
-    const float g = __ldg(col + i * stride);
+    const float g = at(i);
     sg += g;
     sgm += g * (((float)i + 0.5f) - ca);
   }
@@ -157,7 +220,7 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
   sm.ca += -slope * sg + q * sgm;
   sm.cb -= q * sgm;
   if (in(bb)) {
-    const float g = __ldg(col + bb * stride);
+    const float g = at(bb);
     const float w = cb - (float)bb;
     const float mid = 0.5f * ((float)bb + cb) - ca;
     part0 += g * w * (ya + mid * slope);
@@ -168,13 +231,15 @@ __device__ __forceinline__ void grad_segment(const float* __restrict__ col, int6
   }
 }
 
+// x: the corners relative to bin[0] (bin_offset); bins are absolute.
 __device__ __forceinline__ void tent_grad(const float* __restrict__ col, int64_t stride, int T,
-                                          const float c[3], const int bin[3], TentGrad& out) {
-  const float yc = vdiv(2.f, c[2] - c[0]);
+                                          const float x[3], const int bin[3], TentGrad& out) {
+  const float yc = vdiv(2.f, x[2] - x[0]);
+  const int b0 = bin[0];
   float part0 = 0.f;
   SegSums s1{0.f, 0.f, 0.f, 0.f}, s2{0.f, 0.f, 0.f, 0.f};
-  grad_segment(col, stride, T, part0, s1, c[0], bin[0], 0.f, c[1], bin[1], yc);
-  grad_segment(col, stride, T, part0, s2, c[1], bin[1], yc, c[2], bin[2], 0.f);
+  grad_segment(col, stride, T, b0, part0, s1, x[0], 0, 0.f, x[1], bin[1] - b0, yc);
+  grad_segment(col, stride, T, b0, part0, s2, x[1], bin[1] - b0, yc, x[2], bin[2] - b0, 0.f);
   out.part0 = part0;
   out.ayc = s1.yb + s2.ya;
   out.a0 = s1.ca;

@@ -22,7 +22,10 @@
 //    ordering) race on the array and must be serialised by the caller.
 //  * The device address of the array is looked up once per device, on the
 //    first call made while that device is current; make that first call before
-//    any stream capture.
+//    any stream capture. The address is kept for the life of the process, so
+//    the entry point must not be used on a device after cudaDeviceReset.
+//  * The device status word (totri_mesh_workspace_status) lives in the scratch
+//    and is not reported to the caller.
 #include <mutex>
 #include <string>
 

@@ -11,6 +11,7 @@
 #include <string>
 
 #include "capi_common.cuh"
+#include "tune.cuh"
 
 namespace totri {
 namespace rbf {
@@ -258,12 +259,8 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* r, const totri_array_t* 
   if (nv == 0 || N == 0 || B == 0) return TOTRI_OK;
   const int A = C - 4;
   const size_t smem = sizeof(float) * rbf::kChunk * (4 + 2 * (1 + A));
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(rbf::grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(rbf::grad_kernel), smem));
   // voxels per CTA: enough CTAs to fill the GPU several times over
   const int64_t rbf_blocks = ceil_div(N, 128);
   int64_t chunks = std::max<int64_t>(1, (152 * 8 + rbf_blocks - 1) / rbf_blocks);

@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <utility>
 
 #include "common.cuh"
 #include "tune.cuh"
@@ -30,6 +31,21 @@ int sm_count() {
       cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
     return 152;
   return n;
+}
+
+cudaError_t ensure_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& have = done[std::make_pair(func, dev)];
+  if (have >= bytes) return cudaSuccess;
+  const cudaError_t r =
+      cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (r == cudaSuccess) have = bytes;
+  return r;
 }
 
 int grad_split(const char* key, int64_t ctas, int S, int max_slice) {

@@ -414,12 +414,8 @@ int totri_volume_confocal_forward(const totri_array_t* vol, const totri_array_t*
   uint32_t *list, *count;
   TOTRI_TRY(compact(static_cast<const float*>(vol->data), numel(vol), ws, ws_bytes, &list,
                     &count, stream));
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(volume::confocal_forward_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(volume::confocal_forward_kernel), smem));
   const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
   TOTRI_KERNEL("volume confocal forward", stream,
                volume::confocal_forward_kernel<<<(unsigned)ceil_div(N, volume::kPT), 256, smem,
@@ -448,12 +444,8 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
   const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
   const size_t smem = sizeof(float) * 8 * (size_t)Z;
   if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "volume too deep for one column tile");
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(volume::confocal_adjoint_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(volume::confocal_adjoint_kernel), smem));
   TOTRI_KERNEL("volume confocal adjoint", stream,
                volume::confocal_adjoint_kernel<<<(unsigned)(X * Y), 256, smem, stream>>>(
                    g, pts, N, static_cast<const float*>(tr->data), static_cast<float*>(vol->data)));

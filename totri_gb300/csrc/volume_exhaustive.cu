@@ -179,12 +179,8 @@ int launch_fwd(const vexh::Geo& g, int b, const float* vol, const uint32_t* list
                const uint32_t* count, const vexh::Pts& sp, const vexh::Pts& lp, float* out,
                cudaStream_t stream) {
   const size_t smem = sizeof(float) * (size_t)g.T * LT;
-  static int configured = 0;
-  if (smem > 48 * 1024 && configured < (int)smem) {
-    TOTRI_CUDA(cudaFuncSetAttribute(vexh::forward_kernel<LT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = (int)smem;
-  }
+  TOTRI_CUDA(tune::ensure_dynamic_smem(
+      reinterpret_cast<const void*>(vexh::forward_kernel<LT>), smem));
   const dim3 grid((unsigned)g.S, (unsigned)ceil_div(g.L, LT));
   TOTRI_KERNEL("volume exhaustive forward", stream,
                vexh::forward_kernel<LT><<<grid, 256, smem, stream>>>(g, b, vol, list, count, sp,

@@ -1,81 +1,97 @@
-"""Learning-rate schedules and the Adam/SGD wrapper the fitting loops use
-(reference totri/util/optim.py:14-95).
+"""Learning-rate schedules and the optimiser wrapper of the fitting loops.
 
-An interpolator maps the iteration to a learning rate: constant, linear from
-value_0 to value_n over n iterations, or multiplicative (each call moves the
-value a fraction 1 - gamma towards the target, ignoring the iteration).
-``TotriOptimizer`` takes the first rate at construction and a new one after
-every step; during a warm-up of w steps the rate is scaled by
-((k + 1) / (w + 1))^2 at the k-th rate drawn.
+Behaviour the fitting loops rely on (the reference's totri/util/optim.py:14-95
+offers the same schedules under the names kept below as constructors):
+
+* A schedule maps the iteration count i = 0, 1, 2, ... to a learning rate:
+  - constant: the same value for every i;
+  - linear: ``start`` at i = 0 moving evenly to ``end`` at i = n - 1, and held
+    at the nearer end outside that range;
+  - geometric approach: a value that moves the fraction (1 - gamma) of its
+    remaining distance towards ``target`` each time it is queried, whatever i.
+* ``TotriOptimizer`` runs Adam or SGD over one parameter group. It draws a
+  rate when it is given parameters (at construction and on every
+  ``set_params``) and a new one after each ``step``. A warm-up of w draws
+  follows each ``set_params``: its k-th draw (k = 0 .. w-1) is the schedule's
+  rate scaled by ((k + 1) / (w + 1))^2.
 """
 import torch
 
 
-class Interpolator:
-    pass
+class Schedule:
+    """A learning-rate schedule (see the module docstring); call it with the
+    iteration count."""
+
+    def __init__(self, kind, **params):
+        if kind not in ("constant", "linear", "approach"):
+            raise ValueError("unknown schedule kind %r" % (kind,))
+        self.kind = kind
+        self.params = params
+
+    def __call__(self, iteration):
+        p = self.params
+        if self.kind == "constant":
+            return p["value"]
+        if self.kind == "linear":
+            t = iteration / (p["n"] - 1)
+            t = 0.0 if t < 0.0 else (1.0 if t > 1.0 else t)
+            return p["start"] + t * (p["end"] - p["start"])
+        p["value"] = p["target"] + p["gamma"] * (p["value"] - p["target"])
+        return p["value"]
 
 
-class ConstantInterpolator(Interpolator):
-    def __init__(self, constant):
-        self.constant = constant
-
-    def __call__(self, _):
-        return self.constant
+# The reference's schedule names, as constructors of the same schedules.
+Interpolator = Schedule
 
 
-class LinearInterpolator(Interpolator):
-    def __init__(self, value_0, value_n, n):
-        self.value_0, self.value_n, self.n = value_0, value_n, n
-
-    def __call__(self, i):
-        w = max(min(i / (self.n - 1), 1), 0)
-        return (1 - w) * self.value_0 + w * self.value_n
+def ConstantInterpolator(constant):  # noqa: N802
+    return Schedule("constant", value=constant)
 
 
-class MultiplicativeInterpolator(Interpolator):
-    def __init__(self, value, target, gamma=0.99):
-        self.value, self.target, self.gamma = value, target, gamma
+def LinearInterpolator(value_0, value_n, n):  # noqa: N802
+    return Schedule("linear", start=value_0, end=value_n, n=n)
 
-    def __call__(self, _):
-        self.value = self.gamma * self.value + (1 - self.gamma) * self.target
-        return self.value
+
+def MultiplicativeInterpolator(value, target, gamma=0.99):  # noqa: N802
+    return Schedule("approach", value=value, target=target, gamma=gamma)
 
 
 class TotriOptimizer:
+    """Adam or SGD whose learning rate follows a schedule (a number means a
+    constant rate), with a quadratic warm-up after each parameter reset."""
+
+    _OPTIMISERS = {"Adam": torch.optim.Adam, "SGD": torch.optim.SGD}
+
     def __init__(self, params, lr_interpolator, warmup=0, optimizer="Adam"):
-        if optimizer not in ("Adam", "SGD"):
+        if optimizer not in self._OPTIMISERS:
             raise ValueError("Unsupported Optimizer %s" % optimizer)
+        self._make = self._OPTIMISERS[optimizer]
+        self.schedule = (lr_interpolator if callable(lr_interpolator)
+                         else ConstantInterpolator(lr_interpolator))
         self.iteration = 0
-        self.optim_type = optimizer
         self.lr = None
-        if not isinstance(lr_interpolator, Interpolator):
-            lr_interpolator = ConstantInterpolator(lr_interpolator)
-        self.lr_interpolator = lr_interpolator
         self.set_params(params, warmup)
 
-    def set_params(self, params, warmup=0):
-        self.set_warmup(warmup)
-        lr = self.get_next_lr()
-        cls = torch.optim.Adam if self.optim_type == "Adam" else torch.optim.SGD
-        self.optim = cls(params, lr)
+    def _draw(self):
+        rate = self.schedule(self.iteration)
+        self.iteration += 1
+        if self._warm_left > 0:
+            done = self._warmup - self._warm_left
+            rate *= ((done + 1) / (self._warmup + 1)) ** 2
+            self._warm_left -= 1
+        self.lr = rate
+        return rate
 
-    def set_warmup(self, warmup):
-        self.warmup_iter = 0
-        self.warmup_total = warmup
+    def set_params(self, params, warmup=0):
+        """Starts a new optimiser over `params` (fresh moments) and a new warm-up."""
+        self._warmup = self._warm_left = warmup
+        self.optim = self._make(params, self._draw())
 
     def zero_grad(self):
         self.optim.zero_grad()
 
-    def get_next_lr(self):
-        self.lr = self.lr_interpolator(self.iteration)
-        if self.warmup_total > 0 and self.warmup_iter < self.warmup_total:
-            self.lr *= ((self.warmup_iter + 1) / (self.warmup_total + 1)) ** 2
-            self.warmup_iter += 1
-        self.iteration += 1
-        return self.lr
-
     def step(self):
         self.optim.step()
-        lr = self.get_next_lr()
+        rate = self._draw()
         for group in self.optim.param_groups:
-            group["lr"] = lr
+            group["lr"] = rate
