@@ -14,6 +14,7 @@ reference algorithm (oracle/) on the host cores instead (the reference's
 mesh path needs the OptiX SDK and cannot be built).
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -52,6 +53,15 @@ def algorithmic_bytes(kernel, F, S, T, V):
     if kernel == "mesh confocal grad":
         return 64 * F + 12 * S + 4 * T * S + 16 * V
     return None
+
+
+def bench_config(faces, scan_points, bins, world):
+    """The `config` of both arms' JSON lines (the same dict for the same run)."""
+    return {"workload": WORKLOAD, "faces": faces, "scan_points": scan_points, "bins": bins,
+            "pairs_per_step": faces * scan_points,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: flushed between timed steps (256 MiB memset); CPU arm: each step "
+                  "is the whole workload"}
 
 
 def flop_visibility(num_faces):
@@ -340,15 +350,21 @@ def secondary_metrics(device, flush, reps=5):
     }
 
 
-def batched_metrics(device, count=32, steps=2):
+def batched_metrics(device, count=32, steps=2, seed=1234):
     """Batched exhaustive mesh forward + backward: 32 meshes with triangle
     counts log-uniform in [1k, 50k] (lat/long spheres and random boxes),
-    64x64 detector x 16x16 laser points, 2048 bins of 0.005 m; loss
-    0.5 ||transient||^2 per mesh. One graph replay per step (waves within an
-    80 GB transient budget, tiles from the autotuner) against the same work as
-    32 sequential plain calls (forward, then gradient with transient_grad =
-    transient). Unit: (face, detector point, laser point) triples per second."""
-    from totri_gb300 import scenes
+    64x64 detector x 16x16 laser points, 2048 bins of 0.005 m; d loss /
+    d transient of mesh i a seeded N(0, 1) field (totri_fill_normal, seed
+    `seed` + i), loss = <transient, d loss / d transient>. One graph replay
+    per step (waves within an 80 GB budget for the transients and their
+    gradients, tiles from the autotuner) against the same work as 32
+    sequential plain calls (forward, the same N(0, 1) field, gradient). A
+    second line runs the energy head (loss 0.5 ||transient||^2, gradient =
+    transient: one buffer per mesh, larger waves). The plain pass also gives
+    the fraction of its wall time the GPU spends in the library's kernels,
+    which bounds what any batching of these calls can gain. Unit: (face,
+    detector point, laser point) triples per second."""
+    from totri_gb300 import _lib, scenes
     from totri_gb300.batch import BatchedMeshRenderer
     from totri_gb300.totri_cpp import render as R
     s = scenes.batched_exhaustive(count=count)
@@ -368,35 +384,47 @@ def batched_metrics(device, count=32, steps=2):
         e1.synchronize()
         return e0.elapsed_time(e1) / n
 
-    t0 = time.time()
-    br = BatchedMeshRenderer(meshes, sp, bd, laser_points=lp, grad="energy", hbm_budget=80e9)
-    setup_s = time.time() - t0
-    br.step()
-    ms_batched = timed(br.step, steps)
-    waves = [len(w.members) for w in br.waves]
-    tiles = {str(k): v for k, v in br.tiles.items()}
-    from totri_gb300 import _lib
-    # per-kernel times of the same step launched eagerly (graph replays are
-    # not visible to the library's launch profiler)
-    _lib.profile_reset()
-    _lib.profile_enable(True)
-    with torch.cuda.stream(br.stream):
-        br._step_calls()
-    br.stream.synchronize()
-    _lib.profile_enable(False)
-    kernels_batched = {k: {"launches": v[0], "ms": v[2]} for k, v in _lib.profile_read().items()}
-    del br
-    torch.cuda.empty_cache()
+    def batched(head):
+        t0 = time.time()
+        br = BatchedMeshRenderer(meshes, sp, bd, laser_points=lp, grad=head, hbm_budget=80e9,
+                                 normal_seed=seed)
+        setup_s = time.time() - t0
+        br.step()
+        ms = timed(br.step, steps)
+        out = {"ms": ms, "value": triples / (ms / 1e3), "waves": [len(w.members) for w in br.waves],
+               "tiles": {str(k): v for k, v in br.tiles.items()}, "setup_s": setup_s}
+        # per-kernel times of the same step launched eagerly (graph replays are
+        # not visible to the library's launch profiler)
+        _lib.profile_reset()
+        _lib.profile_enable(True)
+        with torch.cuda.stream(br.stream):
+            br._step_calls()
+        br.stream.synchronize()
+        _lib.profile_enable(False)
+        out["kernels_eager"] = {k: {"launches": v[0], "ms": v[2]}
+                                for k, v in _lib.profile_read().items()}
+        del br
+        torch.cuda.empty_cache()
+        return out
+
+    normal = batched("normal")
+    energy = batched("energy")
     so = torch.empty((1, 0, 3), device=device)
+    lib = _lib.load()
 
     def plain():
-        for v, f, m in meshes:
+        for i, (v, f, m) in enumerate(meshes):
             v, f, m = v[None], f[None], m[None]
             out = torch.empty((1, bd.num, S, L), device=device)
             R.mesh_exhaustive_forward(v, f, m, sp[None], lp[None], so, so, out, bd.width,
                                       bd.offset, 0)
+            tg = torch.empty_like(out)
+            _lib.check(lib.totri_fill_normal(ctypes.c_void_p(tg.data_ptr()), tg.numel(),
+                                             seed + i, _lib.stream_of(device)))
+            torch.dot(out.reshape(-1), tg.reshape(-1))
+            del out
             vg, mg = torch.empty_like(v), torch.empty_like(m)
-            R.mesh_exhaustive_grad_verts(v, f, m, sp[None], lp[None], so, so, out, vg, mg,
+            R.mesh_exhaustive_grad_verts(v, f, m, sp[None], lp[None], so, so, tg, vg, mg,
                                          bd.width, bd.offset, 0)
 
     plain()
@@ -405,17 +433,21 @@ def batched_metrics(device, count=32, steps=2):
     ms_plain = timed(plain, 1)
     _lib.profile_enable(False)
     kernels = {k: {"launches": v[0], "ms": v[2]} for k, v in _lib.profile_read().items()}
+    busy = sum(v["ms"] for v in kernels.values()) / ms_plain
     torch.cuda.empty_cache()
     return {
         "kernels_plain_pass": kernels,
-        "kernels_batched_eager": kernels_batched,
-        "value": triples / (ms_batched / 1e3), "unit": "triples/s", "ms": ms_batched,
-        "plain_calls": {"value": triples / (ms_plain / 1e3), "ms": ms_plain},
-        "speedup_vs_plain": ms_plain / ms_batched,
+        "kernels_batched_eager": normal.pop("kernels_eager"),
+        "value": normal["value"], "unit": "triples/s", "ms": normal["ms"],
+        "plain_calls": {"value": triples / (ms_plain / 1e3), "ms": ms_plain,
+                        "gpu_busy_fraction": busy},
+        "speedup_vs_plain": ms_plain / normal["ms"],
+        "speedup_bound_from_idle_gpu": 1.0 / busy if busy > 0 else None,
         "workload": "32 meshes, %d triangles in total (log-uniform 1k-50k), 64x64 detector x "
-                    "16x16 laser points, 2048 bins x 0.005 m, fwd+bwd, energy loss" %
-                    sum(m[1].shape[0] for m in meshes),
-        "waves": waves, "tiles": tiles, "setup_s": setup_s,
+                    "16x16 laser points, 2048 bins x 0.005 m, fwd+bwd, seeded N(0,1) "
+                    "d loss/d transient" % sum(m[1].shape[0] for m in meshes),
+        "waves": normal["waves"], "tiles": normal["tiles"], "setup_s": normal["setup_s"],
+        "energy_head": {k: v for k, v in energy.items() if k != "kernels_eager"},
     }
 
 
@@ -510,13 +542,20 @@ def serve_metrics(device, num_requests=100, seed=0, slots=4):
             fut.result()
         poisson_s = time.perf_counter() - t0
         p50, p99 = srv.latency_ms()
+        breakdown = srv.latency_breakdown()
     kinds = {k: sum(1 for r in reqs if r["kind"] == k) for k in ("render", "grad", "backproject")}
     out = {
         "value": len(reqs) / burst_s, "unit": "requests/s",
         "plain_calls": {"value": len(reqs) / plain_s, "s": plain_s},
         "speedup_vs_plain": plain_s / burst_s,
         "poisson": {"rate_per_s": rate, "p50_ms": p50, "p99_ms": p99,
-                    "throughput": len(reqs) / poisson_s},
+                    "throughput": len(reqs) / poisson_s,
+                    # p50/p99 (ms) of queue wait and service time, all requests
+                    # and per class (small: high-priority streams; large:
+                    # estimated at >= 5 ms of GPU time)
+                    "breakdown": {c: {k: (list(v) if isinstance(v, tuple) else v)
+                                      for k, v in d.items()}
+                                  for c, d in breakdown.items()}},
         "requests": len(reqs), "kinds": kinds, "slots": slots,
         "hbm_budget_gb": 80, "resident_gb": resident / 1e9,
         "peak_admitted_gb": srv.budget.peak / 1e9,
@@ -646,8 +685,7 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_pairs / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "faces": int(s["faces"].shape[1]), "scan_points": S,
-                   "bins": s["bin_def"].num},
+        "config": bench_config(int(s["faces"].shape[1]), S, s["bin_def"].num, args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                          "sample": "%d of %d scan points x all faces per step (BVH visibility, "
                                    "forward, gradient; FP32; OpenMP)" % (n_sub, S)},
@@ -805,10 +843,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "faces": F, "scan_points": S,
-                       "bins": w["bin_def"].num, "pairs_per_step": pairs,
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "flushed between timed steps (256 MiB memset)"},
+            "config": bench_config(F, S, w["bin_def"].num, world),
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -505,6 +505,12 @@ int totri_marching_cubes_grad(const totri_array_t* volume, float iso,
  * edges[256 * 15] edge ids (4 x axis + the other two corner bits), -1 padded. */
 int totri_marching_cubes_table(uint8_t* ntri, int8_t* edges);
 
+/* Fills out[0..n) with standard normal values drawn from `seed`; element i
+ * depends only on (seed, i) (counter-based), so repeated and graph-captured
+ * fills agree. No counterpart in the reference: the batched benchmark's
+ * seeded N(0,1) d loss / d transient. */
+int totri_fill_normal(float* out, int64_t n, uint64_t seed, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -159,6 +159,55 @@ def test_energy_head_in_waves_matches_per_mesh_calls(cuda_lib, tmp_path, monkeyp
             assert rel_l2(grads[i][1].cpu().numpy(), mg[0].cpu().numpy()) < 1e-5
 
 
+def _fill_normal(n, seed):
+    import ctypes
+    from totri_gb300 import _lib
+    out = torch.empty(n, device="cuda")
+    _lib.check(_lib.load().totri_fill_normal(ctypes.c_void_p(out.data_ptr()), n, seed,
+                                             _lib.stream_of(out.device)))
+    return out
+
+
+def test_fill_normal_is_counter_based_and_standard(cuda_lib):
+    """Element i depends on (seed, i) only: a prefix of a longer fill is the
+    shorter fill, seeds differ, and the values are standard normal."""
+    a = _fill_normal(1 << 20, 7)
+    assert torch.equal(_fill_normal(1000, 7), a[:1000])
+    assert not torch.equal(_fill_normal(1000, 8), a[:1000])
+    x = a.double()
+    assert abs(float(x.mean())) < 5e-3 and abs(float(x.std()) - 1.0) < 5e-3
+    assert float((x.abs() > 3.0).double().mean()) == pytest.approx(0.0027, abs=5e-4)
+    assert torch.isfinite(a).all()
+
+
+def test_normal_head_in_waves_matches_per_mesh_calls(cuda_lib, tmp_path, monkeypatch):
+    """The seeded N(0, 1) head: three meshes in two waves; each mesh's
+    transient gradient is the field drawn from seed + its index, so plain calls
+    with the same fill give the same loss <tr, g> and gradients."""
+    monkeypatch.setenv("TOTRI_TUNE_CACHE", str(tmp_path / "tune.json"))
+    meshes = _meshes()
+    sp = scenes.wall_grid(16)[0].cuda()
+    bd = BinDef(0.01, 0.0, 300)
+    budget = 2 * 2 * 4 * bd.num * sp.shape[0] + 1  # two meshes (transient + gradient)
+    br = BatchedMeshRenderer([tuple(t.cuda() for t in m) for m in meshes], sp, bd,
+                             grad="normal", hbm_budget=budget, normal_seed=40)
+    assert len(br.waves) == 2
+    loss = br.step().clone()
+    grads = br.mesh_grads()
+    for i, (v, f, m) in enumerate(meshes):
+        v, f, m = v[None].cuda(), f[None].cuda(), m[None].cuda()
+        empty = torch.empty((1, 0, 3), device="cuda")
+        out = torch.empty((1, bd.num, sp.shape[0]), device="cuda")
+        R.mesh_confocal_forward(v, f, m, sp[None], empty, out, bd.width, bd.offset, 0)
+        tg = _fill_normal(out.numel(), 40 + i).reshape(out.shape)
+        ref = float((out.double() * tg.double()).sum())
+        assert abs(float(loss[i]) - ref) <= 1e-5 * float((out.double() * tg.double()).abs().sum())
+        vg, mg = torch.empty_like(v), torch.empty_like(m)
+        R.mesh_confocal_grad_verts(v, f, m, sp[None], empty, tg, vg, mg, bd.width, bd.offset, 0)
+        assert rel_l2(grads[i][0].cpu().numpy(), vg[0].cpu().numpy()) < 1e-5
+        assert rel_l2(grads[i][1].cpu().numpy(), mg[0].cpu().numpy()) < 1e-5
+
+
 def test_autotune_sweeps_then_reads_cache(cuda_lib, tmp_path, monkeypatch):
     path = tmp_path / "tune.json"
     monkeypatch.setenv("TOTRI_TUNE_CACHE", str(path))

@@ -97,3 +97,21 @@ def test_python_error_mapping(lib):
         _lib.check(_lib.TOTRI_ERR_UNSUPPORTED)
     with pytest.raises(RuntimeError):
         _lib.check(_lib.TOTRI_ERR_CUDA)
+
+
+def test_bounds_checking_build_exports_every_entry_point():
+    """TOTRI_BOUNDS_CHECK=1 builds the bounds-checking variant into its own
+    directory; it exports the same entry points (built and loaded in a child
+    process, since the choice is made when the build module is imported)."""
+    import subprocess
+    import sys
+    code = ("import ctypes, sys; sys.path.insert(0, %r)\n"
+            "from totri_gb300 import build\n"
+            "assert build.bounds_check() and build.BUILD_DIR.endswith('_build_check')\n"
+            "lib = ctypes.CDLL(build.build())\n"
+            "missing = [n for n in %r if not hasattr(lib, n)]\n"
+            "assert not missing, missing\n" % (ROOT, declared_functions()))
+    env = dict(os.environ, TOTRI_BOUNDS_CHECK="1")
+    res = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         timeout=900)
+    assert res.returncode == 0, res.stderr[-2000:]

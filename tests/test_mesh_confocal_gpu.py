@@ -285,24 +285,31 @@ def _with_seed(case, fn):
             autotune.set_tile(k, 0)
 
 
-# (mesh.visibility.queue, mesh.visibility.occupancy): the per-face BVH
-# searches (the default) at 5, 4 and 3 CTAs per SM, and the queued searches at
-# 5 and 4
-_KERNELS = [(0, 0), (0, 4), (0, 1), (1, 0), (1, 4)]
+# visibility kernels: the 4-wide BVH searches (the default) at 4 and 5 CTAs
+# per SM, the binary searches at 5, 4 and 3, and the queued searches at 5 and 4
+_KERNELS = [{}, {"mesh.visibility.occupancy": 5},
+            {"mesh.visibility.wide": 2}, {"mesh.visibility.wide": 2, "mesh.visibility.occupancy": 4},
+            {"mesh.visibility.wide": 2, "mesh.visibility.occupancy": 1},
+            {"mesh.visibility.queue": 1},
+            {"mesh.visibility.queue": 1, "mesh.visibility.occupancy": 4}]
+
+
+@pytest.fixture(scope="module")
+def differentiable_brute_force(cuda_lib):
+    """The full-size workload on the device and its GPU brute-force masks."""
+    d = _dev(scenes.confocal_differentiable())
+    return d, R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
 
 
 @pytest.mark.parametrize("kernel", _KERNELS)
-def test_seeded_visibility_equals_brute_force(cuda_lib, kernel):
+def test_seeded_visibility_equals_brute_force(differentiable_brute_force, kernel):
     """The surface walk from the last occluder of each wall point can only
     prove 'not visible' with the exact leaf test, and the queued BVH searches
     run the same search per ray, so the masks equal the brute-force masks bit
     for bit whatever the walk's settings; full-size 20,480-face workload."""
-    s = scenes.confocal_differentiable()
-    d = _dev(s)
-    bf = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
-    keys = {"mesh.visibility.queue": kernel[0], "mesh.visibility.occupancy": kernel[1]}
+    d, bf = differentiable_brute_force
     for case in _SEED_CASES:
-        got = _with_keys(keys, lambda: _with_seed(case, lambda: R.mesh_visibility(
+        got = _with_keys(kernel, lambda: _with_seed(case, lambda: R.mesh_visibility(
             d["verts"], d["faces"], d["scan_points"])))
         assert torch.equal(got, bf), (kernel, case)
 
@@ -318,15 +325,13 @@ def _with_keys(keys, fn):
             autotune.set_tile(k, 0)
 
 
-def test_shaft_visibility_equals_brute_force(cuda_lib):
+def test_shaft_visibility_equals_brute_force(differentiable_brute_force):
     """The shaft search (one warp-wide BVH walk per target over the hull of
     the warp's wall points and the target's hit box, then exact tests of its
     candidates per lane) gives the brute-force masks bit for bit: with the
     surface walk on or off, with the candidate list capped to force the
     per-lane fallback, and with the wall 40 m away."""
-    s = scenes.confocal_differentiable()
-    d = _dev(s)
-    bf = R.mesh_visibility(d["verts"], d["faces"], d["scan_points"], brute_force=True)
+    d, bf = differentiable_brute_force
     for seed, cap in ((0, 0), (1, 0), (0, 1), (2, 5)):
         got = _with_keys({"mesh.visibility.mode": 7, "mesh.visibility.seed": seed,
                           "mesh.visibility.shaft.cap": cap},
@@ -357,8 +362,7 @@ def test_seeded_visibility_without_or_with_odd_adjacency(cuda_lib, kernel):
     for verts, faces in ((soup_v, soup_f), (v[None].contiguous(), odd_f)):
         ref = oracle.mesh_visibility(verts[0].numpy(), faces[0].numpy(), pts[0].numpy())
         F = faces.shape[1]
-        keys = {"mesh.visibility.queue": kernel[0], "mesh.visibility.occupancy": kernel[1]}
         for case in _SEED_CASES:
-            got = _with_keys(keys, lambda: _with_seed(case, lambda: R.mesh_visibility(
+            got = _with_keys(kernel, lambda: _with_seed(case, lambda: R.mesh_visibility(
                 verts.cuda(), faces.cuda(), pts.cuda())))
             assert np.array_equal(unpack_mask(got[0].cpu().numpy(), F), ref), (kernel, case)

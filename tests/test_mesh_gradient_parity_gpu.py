@@ -238,10 +238,10 @@ def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt):
     assert rel_l2(out[0].double().cpu().numpy(), w["ref"]) < FWD_TOL
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_exhaustive_large_gradient_matches_fp64_oracle(exhaustive_large, mode):
-    """Both gradient kernels (compacted triples, the default, and per-lane mask
-    tests) against the FP64 oracle."""
+    """The three gradient kernels (separable point records, the default;
+    per-lane mask tests; compacted triples) against the FP64 oracle."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]
     empty = torch.empty_like(d["sp"][:, :0])

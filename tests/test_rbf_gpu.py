@@ -67,3 +67,56 @@ def test_full_gaussian_count(cuda_lib):
     vol.backward(vg)
     rg = oracle.rbf2volume_grad(rbf[0].numpy(), ref, vg[0].cpu().numpy(), vd.start, vd.end)
     assert rel(r.grad[0].cpu().numpy(), rg) < 1e-4
+
+
+def _with_cull(off, fn):
+    from totri_gb300 import autotune
+    autotune.set_tile("rbf.cull", 1 if off else 0)
+    try:
+        return fn()
+    finally:
+        autotune.set_tile("rbf.cull", 0)
+
+
+@pytest.mark.parametrize("attrs", [0, 1, 3])
+def test_underflow_cull_is_bit_identical(cuda_lib, attrs):
+    """Gaussians whose ex2 value underflows to zero over a whole voxel brick
+    are skipped; the forward stays bit for bit the same (zero terms, same
+    order), also with non-finite and degenerate Gaussians in the set and a
+    grid that does not divide into bricks, and the gradient (summed with
+    atomics, so only equal up to their order) agrees to FP32 rounding."""
+    from totri_gb300.totri_cpp import util as U
+    rng = np.random.default_rng(40 + attrs)
+    N = 700
+    rbf = np.concatenate([rng.uniform(-0.5, 0.5, (N, 3)) + np.array([0, 0, 1.0]),
+                          rng.uniform(0.01, 0.05, (N, 1)), rng.random((N, attrs))], 1)
+    rbf = rbf.astype(np.float32)
+    rbf[5, 0] = np.inf          # a non-finite centre is never culled
+    rbf[9, 3] = 0.0             # sigma 0: infinite exponent constant
+    if attrs:
+        rbf[11, 4] = np.nan     # a non-finite attribute is never culled
+    r = torch.as_tensor(rbf[None]).cuda()
+    shape = (37, 21, 19)
+    start, end = (-0.5, -0.5, 0.5), (0.5, 0.5, 1.5)
+
+    def fwd():
+        v = torch.full((1, 1 + attrs) + shape, 7.0, device="cuda")
+        U.rbf2volume_gaussian_forward(r, v, start, end)
+        return v
+
+    on, off = fwd(), _with_cull(True, fwd)
+    assert torch.equal(torch.nan_to_num(on, nan=1234.5), torch.nan_to_num(off, nan=1234.5))
+    assert torch.equal(torch.isnan(on), torch.isnan(off))
+
+    ok = np.isfinite(rbf).all(1) & (rbf[:, 3] > 0)  # the gradient on finite Gaussians
+    r = torch.as_tensor(rbf[ok][None]).cuda()
+    vol = fwd()
+    vg = torch.randn_like(vol)
+
+    def grad():
+        g = torch.zeros_like(r)
+        U.rbf2volume_gaussian_grad(r, vol, vg, g, start, end)
+        return g
+
+    g_on, g_off = grad(), _with_cull(True, grad)
+    assert rel(g_on.cpu().numpy(), g_off.cpu().numpy()) < 1e-6

@@ -89,14 +89,50 @@ def test_results_same_alone_and_in_the_mix(cuda_lib):
     with _server(meshes, grids, slots=1) as srv:
         for r in reqs:
             alone.append(srv.submit(_clone(r)).result(timeout=120))
-    with _server(meshes, grids, slots=4) as srv:
+    # a low threshold sends part of the mix to the normal-priority streams
+    with _server(meshes, grids, slots=4, large_slots=2, large_ms=0.02) as srv:
         futs = [srv.submit(_clone(r)) for r in reqs * 3]  # each request three times
         mixed = [f.result(timeout=300) for f in futs]
         p50, p99 = srv.latency_ms()
         assert p50 is not None and p99 >= p50
         assert srv.budget.peak <= srv.budget.total
+        br = srv.latency_breakdown()
+        assert br["small"]["requests"] > 0 and br["large"]["requests"] > 0
+        assert br["all"]["requests"] == len(futs)
+        for cls in ("small", "large"):
+            wait, service = br[cls]["wait"], br[cls]["service"]
+            assert wait[0] >= 0 and service[0] > 0 and service[1] >= service[0]
     for i, r in enumerate(reqs * 3):
         _compare(r.kind, mixed[i], alone[i % len(reqs)])
+
+
+def test_cancelled_requests_release_their_memory(cuda_lib):
+    """A request cancelled while queued never runs; one cancelled in flight
+    runs to its end on the GPU, its result is dropped, its device memory
+    returns to the budget and its visibility mask is unpinned; the server then
+    serves the next request. The scheduler's steps are driven by hand here, so
+    the request is certainly in flight when it is cancelled."""
+    meshes, grids = _scene()
+    srv = _server(meshes, grids)
+    queued = srv.submit(Request("render", "g16", mesh="ico", bins=BINS))
+    assert queued.cancel()
+    flight = srv.submit(Request("grad", "g24", mesh="bumpy", bins=BINS2, target="g24_b"))
+    with srv.cv:
+        assert srv._admit_one()  # drops the cancelled request
+        assert len(srv.queue) == 1 and not srv.inflight
+        assert srv._admit_one()
+        assert len(srv.inflight) == 1 and srv.budget.inflight > 0
+        assert srv.masks.pins
+        assert flight.cancel()
+        torch.cuda.synchronize()
+        assert srv._reap()
+    assert srv.cancelled == 1 and not srv.completed
+    assert srv.budget.inflight == 0 and not srv.masks.pins
+    assert queued.cancelled() and flight.cancelled()
+    with srv:
+        ok = srv.submit(Request("render", "g16", mesh="ico", bins=BINS))
+        assert ok.result(timeout=60).shape == (BINS.num, 256)
+    assert srv.budget.inflight == 0
 
 
 def test_results_match_plain_calls(cuda_lib):

@@ -78,6 +78,7 @@ _SIGNATURES = {
     "totri_last_error": [],
     "totri_tune_set": [ctypes.c_char_p, _int],
     "totri_tune_get": [ctypes.c_char_p],
+    "totri_fill_normal": [_vp, _i64, ctypes.c_uint64, _vp],
     "totri_profile_enable": [_int],
     "totri_profile_reset": [],
     "totri_profile_read": [_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64),

@@ -15,6 +15,10 @@ Loss heads (``grad``):
     batch must fit one wave (the gradient of every mesh is held at once);
   * ``"energy"`` — loss = 0.5 * ||transient||^2 per mesh, whose gradient is
     the transient itself (no second transient-sized buffer); any wave count;
+  * ``"normal"`` — d loss / d transient of mesh i is a standard normal field
+    drawn from seed ``normal_seed + i`` (``totri_fill_normal``: the same values
+    for any wave packing), loss = <transient, d loss / d transient>; any wave
+    count;
   * a callable ``fn(wave_meshes, transient, transient_grad)`` run inside the
     capture (torch ops on the device), which fills ``transient_grad`` for the
     meshes of the wave (indices into the constructor's list).
@@ -24,6 +28,7 @@ only while this renderer launches its own kernels and handed back to the
 built-in choices afterwards; captured graphs keep the values they were
 captured with. Renderers on several threads must not launch concurrently.
 """
+import ctypes
 import math
 import typing
 
@@ -64,12 +69,13 @@ class BatchedMeshRenderer:
     def __init__(self, meshes: typing.Sequence, scan_points: torch.Tensor, bin_def: BinDef,
                  laser_points: typing.Optional[torch.Tensor] = None, device=None,
                  grad="external", hbm_budget: float = 80e9, graph: bool = True,
-                 tune: bool = True):
+                 tune: bool = True, normal_seed: int = 0):
         self.device = dev = torch.device(device or "cuda")
         self.lib = _lib.load()
         self.bin_def = bin_def
         self.exhaustive = laser_points is not None
         self.grad = grad
+        self.normal_seed = int(normal_seed)
         self.sizes = [(m[0].shape[0], m[1].shape[0]) for m in meshes]
         S = scan_points.shape[0]
         T = bin_def.num
@@ -199,6 +205,16 @@ class BatchedMeshRenderer:
         if self.grad == "energy":
             sq = torch.linalg.vector_norm(tr.reshape(n, -1), dim=1)
             self.loss.index_copy_(0, w.member_ids, 0.5 * sq * sq)
+        elif self.grad == "normal":
+            tg = self.transient_grad[:n]
+            for pos, i in enumerate(w.members):
+                _lib.check(self.lib.totri_fill_normal(
+                    ctypes.c_void_p(tg[pos].data_ptr()), tg[pos].numel(),
+                    self.normal_seed + i, _lib.stream_of(self.device)))
+            # one dot product per mesh (no transient-sized temporary)
+            dots = torch.stack([torch.dot(tr[p].reshape(-1), tg[p].reshape(-1))
+                                for p in range(n)])
+            self.loss.index_copy_(0, w.member_ids, dots)
         elif callable(self.grad):
             self.grad(list(w.members), tr, self.transient_grad[:n])
 
@@ -251,7 +267,8 @@ class BatchedMeshRenderer:
     def step(self, transient_grad: typing.Optional[torch.Tensor] = None):
         """Forward + loss head + backward for every mesh. With grad='external',
         `transient_grad` (rows in wave order) is copied in first. Returns the
-        per-mesh loss (energy head) or None; gradients via ``mesh_grads()``."""
+        per-mesh loss (energy and normal heads) or None; gradients via
+        ``mesh_grads()``."""
         if transient_grad is not None:
             if self.grad != "external":
                 raise ValueError("transient_grad is given only with grad='external'")
@@ -263,7 +280,7 @@ class BatchedMeshRenderer:
             with torch.cuda.stream(self.stream):
                 self._step_calls()
         self.stream.synchronize()
-        return self.loss if self.grad == "energy" else None
+        return self.loss if self.grad in ("energy", "normal") else None
 
     def wave_order(self):
         """Constructor indices of the transient rows of a one-wave batch."""

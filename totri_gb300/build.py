@@ -4,6 +4,11 @@ Each translation unit in csrc/ is compiled by nvcc in parallel into _build/,
 then linked into totri_gb300/_build/libtotri_gb300.so with the CUDA runtime
 linked statically. The build is incremental (object files newer than their
 source and the shared headers are reused).
+
+With TOTRI_BOUNDS_CHECK=1 in the environment the bounds-checking variant is
+built instead, into _build_check/ (-DTOTRI_BOUNDS_CHECK: the indices the
+kernels take from device data are checked, an out-of-range one raises a device
+status bit and is clamped), and the loader picks that library.
 """
 import concurrent.futures as cf
 import glob
@@ -15,9 +20,17 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-BUILD_DIR = os.path.join(PKG, "_build")
 LIB_NAME = "libtotri_gb300.so"
+
+
+def bounds_check():
+    """True when TOTRI_BOUNDS_CHECK=1 selects the bounds-checking build."""
+    return os.environ.get("TOTRI_BOUNDS_CHECK", "") not in ("", "0")
+
+
+BUILD_DIR = os.path.join(PKG, "_build_check" if bounds_check() else "_build")
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
+CHECK_FLAGS = ["-DTOTRI_BOUNDS_CHECK"] if bounds_check() else []
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -41,7 +54,7 @@ def _compile(src, extra, verbose):
     deps = [src, __file__] + _headers()
     if os.path.exists(obj) and all(os.path.getmtime(d) <= os.path.getmtime(obj) for d in deps):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj + ".tmp"]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *CHECK_FLAGS, *extra, "-c", src, "-o", obj + ".tmp"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     res = subprocess.run(cmd, capture_output=True, text=True)

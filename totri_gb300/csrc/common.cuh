@@ -45,11 +45,26 @@ int cuda_status(cudaError_t e, const char* what);
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Device status bits written into a workspace header.
+// Device status bits written into a workspace header. kStatusFaceIndexRange
+// reports an input (a face index >= V ends the face list); the other two are
+// internal errors: a BVH search that hit its step or stack limit, and (in
+// the bounds-checking build only) an index read from device data that was
+// out of range.
 enum : uint32_t {
   kStatusFaceIndexRange = 1u,
   kStatusTraversalCap = 2u,
+  kStatusIndexRange = 4u,
 };
+
+// TOTRI_INDEX_OK(cond, status): in the bounds-checking build (TOTRI_BOUNDS_CHECK)
+// evaluates cond and, when it fails, sets kStatusIndexRange in *status; the
+// caller clamps or skips the access. Otherwise it is `true` and costs nothing.
+#ifdef TOTRI_BOUNDS_CHECK
+#define TOTRI_INDEX_OK(cond, status) \
+  ((cond) ? true : (atomicOr((status), ::totri::kStatusIndexRange), false))
+#else
+#define TOTRI_INDEX_OK(cond, status) true
+#endif
 
 // ---------------------------------------------------------------------------
 // Strided views of small input arrays (element strides).

@@ -606,6 +606,143 @@ __device__ __forceinline__ bool bvh_occluded(const Scene& sc, int b, int n, int 
   }
 }
 
+// bvh_occluded over the 4-wide tree (see target_visible_pp4 for its records):
+// one step tests the four child boxes of a record, whose planes are SoA
+// float4s, with twelve paired FMAs, goes on with the nearest hit and stacks
+// the others. kOct as in node_slabs. The leaves tested, and so the answer,
+// are those of bvh_occluded: a leaf is reached iff its binary ancestors' boxes
+// and its own all pass.
+// Code of an unused slot of a 4-wide record.
+constexpr int kWideEmpty = INT_MIN + 1;
+
+template <int kOct>
+__device__ __forceinline__ bool bvh_occluded_wide_oct(const Scene& sc, int b, int n, int k, int f,
+                                                      fv3 o, fv3 dir, float tmax, float tf,
+                                                      fv3 inv, fv3 oinv, uint32_t* status,
+                                                      int& seed) {
+  constexpr int kDone = INT_MIN;
+  const unsigned long long ix = f2pack(inv.x, inv.x), iy = f2pack(inv.y, inv.y),
+                           iz = f2pack(inv.z, inv.z);
+  const unsigned long long nx = f2pack(-oinv.x, -oinv.x), ny = f2pack(-oinv.y, -oinv.y),
+                           nz = f2pack(-oinv.z, -oinv.z);
+  const float4* wb = sc.wide + (size_t)b * sc.F * 8;
+  int stack[64];
+  int sp = 0;
+  auto pop = [&]() { return sp > 0 ? stack[--sp] : kDone; };
+  auto push = [&](int v) {
+    if (sp < 64) stack[sp++] = v;
+    else atomicOr(status, kStatusTraversalCap);
+  };
+  int node = 0;
+  int leaf = kDone;
+  const unsigned inner = (unsigned)(n - 1);
+  int budget = 2 * n + 64;
+  while (node != kDone) {
+    while (node >= 0) {
+      if (--budget < 0 || (unsigned)node >= inner) {
+        atomicOr(status, kStatusTraversalCap);
+        return false;
+      }
+      const float4* w = wb + (size_t)node * 8;
+      const float4 lx = __ldg(w), ly = __ldg(w + 1), lz = __ldg(w + 2);
+      const float4 hx = __ldg(w + 3), hy = __ldg(w + 4), hz = __ldg(w + 5);
+      const float4 cc = __ldg(w + 6);
+      float lx0, lx1, lx2, lx3, ly0, ly1, ly2, ly3, lz0, lz1, lz2, lz3;
+      float hx0, hx1, hx2, hx3, hy0, hy1, hy2, hy3, hz0, hz1, hz2, hz3;
+      f2unpack(f2fma(f2pack(lx.x, lx.y), ix, nx), lx0, lx1);
+      f2unpack(f2fma(f2pack(lx.z, lx.w), ix, nx), lx2, lx3);
+      f2unpack(f2fma(f2pack(ly.x, ly.y), iy, ny), ly0, ly1);
+      f2unpack(f2fma(f2pack(ly.z, ly.w), iy, ny), ly2, ly3);
+      f2unpack(f2fma(f2pack(lz.x, lz.y), iz, nz), lz0, lz1);
+      f2unpack(f2fma(f2pack(lz.z, lz.w), iz, nz), lz2, lz3);
+      f2unpack(f2fma(f2pack(hx.x, hx.y), ix, nx), hx0, hx1);
+      f2unpack(f2fma(f2pack(hx.z, hx.w), ix, nx), hx2, hx3);
+      f2unpack(f2fma(f2pack(hy.x, hy.y), iy, ny), hy0, hy1);
+      f2unpack(f2fma(f2pack(hy.z, hy.w), iy, ny), hy2, hy3);
+      f2unpack(f2fma(f2pack(hz.x, hz.y), iz, nz), hz0, hz1);
+      f2unpack(f2fma(f2pack(hz.z, hz.w), iz, nz), hz2, hz3);
+      auto box = [&](float ax, float ay, float az, float bx, float by, float bz, float& t) {
+        float a, e;
+        if (kOct == 8) {
+          a = fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz));
+          e = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tf));
+        } else {
+          constexpr bool qx = kOct & 1, qy = kOct & 2, qz = kOct & 4;
+          a = fmax3(qx ? bx : ax, qy ? by : ay, qz ? bz : az);
+          e = fmin3(qx ? ax : bx, qy ? ay : by, fminf(qz ? az : bz, tf));
+        }
+        t = a;
+        return a <= e;
+      };
+      const int c0 = __float_as_int(cc.x), c1 = __float_as_int(cc.y);
+      const int c2 = __float_as_int(cc.z), c3 = __float_as_int(cc.w);
+      float t0, t1, t2, t3;
+      const bool h0 = box(lx0, ly0, lz0, hx0, hy0, hz0, t0);
+      const bool h1 = box(lx1, ly1, lz1, hx1, hy1, hz1, t1) && c1 != kWideEmpty;
+      const bool h2 = box(lx2, ly2, lz2, hx2, hy2, hz2, t2) && c2 != kWideEmpty;
+      const bool h3 = box(lx3, ly3, lz3, hx3, hy3, hz3, t3) && c3 != kWideEmpty;
+      float best = INFINITY;
+      int next = kDone;
+      if (h0 && t0 < best) { best = t0; next = c0; }
+      if (h1 && t1 < best) { best = t1; next = c1; }
+      if (h2 && t2 < best) { best = t2; next = c2; }
+      if (h3 && t3 < best) { best = t3; next = c3; }
+      if (h3 && next != c3) push(c3);
+      if (h2 && next != c2) push(c2);
+      if (h1 && next != c1) push(c1);
+      if (h0 && next != c0) push(c0);
+      node = next != kDone ? next : pop();
+      if (node < 0 && node != kDone && leaf == kDone) {
+        leaf = node;
+        node = pop();
+      }
+      if (!__any_sync(__activemask(), leaf == kDone)) break;
+    }
+    while (leaf != kDone) {
+      const int kk = ~leaf;
+      if (kk != k) {
+        if (kk < 0 || kk >= n) {
+          atomicOr(status, kStatusTraversalCap);
+        } else {
+          const float4* q = tri_at(sc, b, kk);
+          const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+          float tq;
+          if (tri_hit(q0, q1, q2, q3, o, dir, tmax, tq) &&
+              (tq < tf || (tq == tf && __float_as_int(q3.w) < f))) {
+            seed = kk;
+            return true;
+          }
+        }
+      }
+      leaf = kDone;
+      if (node < 0 && node != kDone) {
+        leaf = node;
+        node = pop();
+      }
+    }
+  }
+  return false;
+}
+
+// bvh_occluded through the 4-wide tree, with the same octant dispatch.
+__device__ __forceinline__ bool bvh_occluded_wide(const Scene& sc, int b, int n, int k, int f,
+                                                  fv3 o, fv3 dir, float tmax, float tf,
+                                                  uint32_t* status, int& seed) {
+  const fv3 inv = mkv(safe_inv(dir.x), safe_inv(dir.y), safe_inv(dir.z));
+  const fv3 oinv = mkv(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+  const unsigned act = __activemask();
+  const int oct = ray_octant(inv);
+  const int lead = __shfl_sync(act, oct, __ffs(act) - 1);
+  const int mode = __all_sync(act, oct == lead) && lead < 4 ? lead : 8;
+  switch (mode) {
+    case 0: return bvh_occluded_wide_oct<0>(sc, b, n, k, f, o, dir, tmax, tf, inv, oinv, status, seed);
+    case 1: return bvh_occluded_wide_oct<1>(sc, b, n, k, f, o, dir, tmax, tf, inv, oinv, status, seed);
+    case 2: return bvh_occluded_wide_oct<2>(sc, b, n, k, f, o, dir, tmax, tf, inv, oinv, status, seed);
+    case 3: return bvh_occluded_wide_oct<3>(sc, b, n, k, f, o, dir, tmax, tf, inv, oinv, status, seed);
+    default: return bvh_occluded_wide_oct<8>(sc, b, n, k, f, o, dir, tmax, tf, inv, oinv, status, seed);
+  }
+}
+
 __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
                                                   const Target& tg, fv3 o, uint32_t* status,
                                                   int& seed, int seed_mode, int seed_steps) {
@@ -748,7 +885,6 @@ __device__ __forceinline__ int shaft_candidates(const Scene& sc, int b, int n, i
 // answer, are those of target_visible: a leaf is reached iff its binary
 // ancestors' boxes and its own all pass, and the grandchild boxes are the same
 // boxes the binary walk tests.
-constexpr int kWideEmpty = INT_MIN + 1;
 
 __device__ __forceinline__ bool target_visible_pp4(const Scene& sc, int b, int n,
                                                    const Target& tg, fv3 o, uint32_t* status) {

@@ -312,7 +312,8 @@ __global__ void records_kernel(Scene sc, BuildInputs in) {
   const Meta& m = sc.meta[b];
   const int n = m.n;
   if (k >= n) return;
-  const int f = (int)sc.vals[(size_t)b * 2 * sc.F + (size_t)sc.sorted_buf * sc.F + k];
+  int f = (int)sc.vals[(size_t)b * 2 * sc.F + (size_t)sc.sorted_buf * sc.F + k];
+  if (!TOTRI_INDEX_OK((unsigned)f < (unsigned)in.F, sc.status)) f = 0;
   fv3 v[3];
   int64_t idx[3];
   face_verts(in, b, f, v, idx);

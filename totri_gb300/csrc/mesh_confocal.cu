@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(256) visibility_kernel(Scene sc, View3f pts, i
 constexpr int kMaxPatchChunks = 16;
 
 // kWalk 0: target_visible_pp, 1: packet_visible, 2: target_visible_pp4, 3: shaft
-// search; kOcc: CTAs per SM that the register allocation must allow.
+// search, 4: target_visible_pp's prefix and a 4-wide BVH search
+// (bvh_occluded_wide); kOcc: CTAs per SM that the register allocation must allow.
 template <int kWalk, int kOcc = 1>
 __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, View3f pts, int P,
                                                                int row0, int chunks,
@@ -131,7 +132,8 @@ __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, V
   const int n = sc.meta[b].n;
   const bool okp = i < P;
   const uint32_t* order = sc.pscratch + 3 * (size_t)sc.B * P + (size_t)b * P;
-  const int p = okp ? (int)order[i] : 0;
+  int p = okp ? (int)order[i] : 0;
+  if (!TOTRI_INDEX_OK((unsigned)p < (unsigned)P, sc.status)) p = 0;
   const fv3 o = okp ? mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2)) : mkv(0.f, 0.f, 0.f);
   volatile int* vseeds = seeds;
   volatile int* gseeds = reinterpret_cast<int*>(sc.pscratch) + (size_t)b * P;
@@ -221,6 +223,16 @@ __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, V
           }
         }
         if (okp && seed != s0) vseeds[lane] = seed;
+      } else if (kWalk == 4) {
+        if (okp) {
+          const int s0 = vseeds[lane];
+          int seed = s0;
+          fv3 dir;
+          float tmax, tf;
+          if (query_prefix(sc, b, n, tg, o, seed, seed_mode, seed_steps, dir, tmax, tf, vis))
+            vis = !bvh_occluded_wide(sc, b, n, tg.k, tg.f, o, dir, tmax, tf, sc.status, seed);
+          if (seed != s0) vseeds[lane] = seed;
+        }
       } else if (okp) {
         const int s0 = vseeds[lane];
         int seed = s0;
@@ -232,7 +244,7 @@ __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, V
     if (lane == 0) bits[c][j] = w;
   }
   __syncthreads();
-  if (threadIdx.x < 32 && okp && (kWalk == 0 || kWalk == 3)) gseeds[i] = seeds[lane];
+  if (threadIdx.x < 32 && okp && (kWalk == 0 || kWalk == 3 || kWalk == 4)) gseeds[i] = seeds[lane];
   for (int c = warp; c < nc; c += 8) {
     if (!okp) continue;
     uint32_t word = 0u;
@@ -274,7 +286,8 @@ __global__ void __launch_bounds__(256, kOcc) visibility_queue_kernel(Scene sc, V
   const int n = sc.meta[b].n;
   const bool okp = i < P;
   const uint32_t* order = sc.pscratch + 3 * (size_t)sc.B * P + (size_t)b * P;
-  const int p = okp ? (int)order[i] : 0;
+  int p = okp ? (int)order[i] : 0;
+  if (!TOTRI_INDEX_OK((unsigned)p < (unsigned)P, sc.status)) p = 0;
   const fv3 o = okp ? mkv(pts.at(b, p, 0), pts.at(b, p, 1), pts.at(b, p, 2)) : mkv(0.f, 0.f, 0.f);
   volatile int* vseeds = seeds;
   volatile int* gseeds = reinterpret_cast<int*>(sc.pscratch) + (size_t)b * P;
@@ -712,6 +725,7 @@ __global__ void mask_unsort_kernel(Scene sc, int P, uint32_t* out) {
   const uint32_t w = sc.mask[((size_t)b * sc.P + p) * sc.nch + (k >> 5)];
   if (!((w >> (k & 31)) & 1u)) return;
   const int f = __float_as_int(tri_at(sc, b, k)[3].w);
+  if (!TOTRI_INDEX_OK((unsigned)f < (unsigned)sc.F, sc.status)) return;
   atomicOr(out + ((size_t)b * P + p) * sc.nch + (f >> 5), 1u << (f & 31));
 }
 
@@ -779,6 +793,22 @@ int launch_visibility(const Scene& sc, const View3f& pts, int P, int row0, bool 
       TOTRI_KERNEL("mesh visibility", stream,
                    visibility_patch_kernel<3><<<grid, 256, 0, stream>>>(
                        sc, pts, P, row0, chunks, seed_mode, seed_steps, shaft_cap));
+    // The default: the surface-walk prefix, then the 4-wide BVH search
+    // (bvh_occluded_wide) with registers for 4 CTAs per SM (60, no spills):
+    // 8.81 ms against 9.19 ms for the binary search at 5 CTAs per SM (48
+    // registers, spilling) and 9.26 ms for the 4-wide search capped at 5, per
+    // mesh_visibility call on the differentiable workload (build included).
+    // "mesh.visibility.wide" = 2 selects the binary search.
+    else if (tune::get("mesh.visibility.wide") != 2 && tune::get("mesh.visibility.queue") != 1) {
+      if (tune::get("mesh.visibility.occupancy") == 5)
+        TOTRI_KERNEL("mesh visibility", stream,
+                     visibility_patch_kernel<4, 5><<<grid, 256, 0, stream>>>(
+                         sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
+      else
+        TOTRI_KERNEL("mesh visibility", stream,
+                     visibility_patch_kernel<4, 4><<<grid, 256, 0, stream>>>(
+                         sc, pts, P, row0, chunks, seed_mode, seed_steps, 0));
+    }
     // The queued BVH searches (visibility_queue_kernel) when
     // "mesh.visibility.queue" = 1; queue entries pack the target's Morton
     // position in 26 bits.

@@ -460,6 +460,288 @@ __global__ void __launch_bounds__(256) exh_grad_compact_kernel(
   }
 }
 
+// Gradient that uses the separability of the triple terms. For one face,
+// everything that depends on the scan point s alone or the laser point l alone
+// is computed once per point into a shared-memory record:
+//   - the exact FP32 lengths |v_m - p| that decide the vertex order and bins
+//     (the same chain as exh_pair) and their double-float low parts;
+//   - the origin term |p - o_p| (exact FP32 and low part);
+//   - the point's alpha factor A_p = max(0, r.z) |n.r| / |r|^4 (r = c - p),
+//     with alpha = 100 rho |n|^-1 A_s A_l (AlphaExhaustive, mesh_common.h:505-531);
+//   - its parts of d log(alpha) / d v_m: cm = -4/3 r/|r|^2 + n/(3 n.r) +
+//     (0, 0, 1/(3 r.z)), the same for every vertex, and wv = r/(n.r), which
+//     enters through the normal's Jacobian (AlphaExhaustiveGradVerts,
+//     mesh_common.h:549-630);
+//   - the unit vectors u_m = (v_m - p)/|v_m - p| that make up d c_k / d v.
+// A triple then only combines two records: the alpha gradient is taken in the
+// face's own vertex order (the formula is the same in any order), and only
+// the tent terms follow the sorted order. A CTA takes its faces one at a time
+// over a slice of at most kFaceSlice scan points and the lasers in chunks of
+// kFaceSlice; its 256 threads share each face's (s, l) pairs. The decisions
+// (vertex order, bins) are those of exh_pair.
+constexpr int kFaceSlice = 256;
+constexpr int kFacesPerCta = 8;
+constexpr int kRec = 24;  // floats per point record (fields below)
+enum : int {
+  kRecD = 0,     // [3] exact FP32 lengths
+  kRecDlo = 3,   // [3] their low parts
+  kRecOd = 6,    // origin term, FP32
+  kRecOdlo = 7,  // its low part
+  kRecA = 8,     // alpha factor
+  kRecCm = 9,    // [3]
+  kRecWv = 12,   // [3]
+  kRecU = 15,    // [9] unit vectors u_m
+};
+
+// Fills the record of point p (origin o if has_o) for the face (v, c, n);
+// rec[f * stride] is field f.
+__device__ __forceinline__ void exh_point_record(const fv3 v[3], fv3 c, fv3 n, fv3 p, bool has_o,
+                                                 fv3 o, float* rec, int stride) {
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const float d = xlen(xsub3(v[m], p));
+    const DFloat df = len_df(v[m], p);
+    rec[(kRecD + m) * stride] = d;
+    rec[(kRecDlo + m) * stride] = (df.hi - d) + df.lo;
+    const float inv = vdiv(1.f, d);
+    const fv3 u = inv * (v[m] - p);
+    rec[(kRecU + 3 * m) * stride] = u.x;
+    rec[(kRecU + 3 * m + 1) * stride] = u.y;
+    rec[(kRecU + 3 * m + 2) * stride] = u.z;
+  }
+  float od = 0.f, odlo = 0.f;
+  if (has_o) {
+    od = xlen(xsub3(p, o));
+    const DFloat df = len_df(p, o);
+    odlo = (df.hi - od) + df.lo;
+  }
+  rec[kRecOd * stride] = od;
+  rec[kRecOdlo * stride] = odlo;
+  const fv3 r = c - p;
+  const float rr = dot(r, r), nr = dot(n, r);
+  const bool front = r.z > 0.f;
+  rec[kRecA * stride] = front ? vdiv(r.z * fabsf(nr), rr * rr) : 0.f;
+  const float kr = vdiv(-4.f, 3.f * rr), knr = vdiv(1.f, nr), kw = vdiv(1.f, 3.f * r.z);
+  const fv3 cm = kr * r + (knr * (1.f / 3.f)) * n + mkv(0.f, 0.f, front ? kw : 0.f);
+  rec[kRecCm * stride] = cm.x;
+  rec[(kRecCm + 1) * stride] = cm.y;
+  rec[(kRecCm + 2) * stride] = cm.z;
+  rec[kRecWv * stride] = knr * r.x;
+  rec[(kRecWv + 1) * stride] = knr * r.y;
+  rec[(kRecWv + 2) * stride] = knr * r.z;
+}
+
+// Block-wide compaction: returns this thread's slot among the threads whose
+// flag is set (or -1) and leaves their count in *total. All 256 threads call it.
+__device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned bal = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) warp_counts[warp] = __popc(bal);
+  __syncthreads();
+  int base = 0, sum = 0;
+  for (int w = 0; w < 8; ++w) {
+    const int c = warp_counts[w];
+    base += w < warp ? c : 0;
+    sum += c;
+  }
+  *total = sum;
+  return flag ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
+}
+
+__global__ void __launch_bounds__(256, 3) exh_grad_face_kernel(
+    Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
+    int T, float bw, float bo, GradOut out) {
+  extern __shared__ float recs[];        // scan-point then laser-point records, SoA
+  float* srec = recs;
+  float* lrec = recs + kRec * kFaceSlice;
+  __shared__ short sidx[kFaceSlice], lidx[kFaceSlice];
+  __shared__ int counts[2][8];
+  __shared__ float red[8][10];
+  const int b = blockIdx.y;
+  const int n = sc.meta[b].n;
+  const int s0 = blockIdx.z * kFaceSlice;
+  const int ns_all = min(kFaceSlice, S - s0);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float* tgb = tgrad + (size_t)b * T * S * L;
+  const int64_t stride = (int64_t)S * L;
+  const float4* shade = sc.shade + (size_t)b * sc.F * 4;
+  const uint32_t* mrows = sc.mask + (size_t)b * sc.P * sc.nch;
+  const float inv_bw = __frcp_rn(bw);
+  for (int fi = 0; fi < kFacesPerCta; ++fi) {
+    const int k = blockIdx.x * kFacesPerCta + fi;
+    if (k >= n) break;  // CTA-uniform
+    const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
+    const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
+    const fv3 v[3] = {mkv(s0r.x, s0r.y, s0r.z), mkv(s1r.x, s1r.y, s1r.z), mkv(s2r.x, s2r.y, s2r.z)};
+    const fv3 c = mkv(s3r.x, s3r.y, s3r.z);
+    const fv3 e1 = v[1] - v[0], e2 = v[2] - v[0];
+    const fv3 nrm = cross(e1, e2);
+    const float nn = dot(nrm, nrm);
+    const float rho = s0r.w;
+    const float kf = 100.f * rho * rsqrtf(nn);
+    const fv3 wf = vdiv(-1.f, nn) * nrm;
+    const int ch = k >> 5;
+    const uint32_t bit = 1u << (k & 31);
+    // the face's scan-point records over this slice
+    int ns;
+    {
+      const int s = s0 + tid;
+      const bool vis = tid < ns_all && (mrows[(size_t)s * sc.nch + ch] & bit);
+      const int at = block_slot(vis, counts[0], &ns);
+      if (vis) {
+        const fv3 p = mkv(sp.at(b, s, 0), sp.at(b, s, 1), sp.at(b, s, 2));
+        const fv3 o = org.has_so ? mkv(org.so.at(b, s, 0), org.so.at(b, s, 1), org.so.at(b, s, 2))
+                                 : mkv(0.f, 0.f, 0.f);
+        exh_point_record(v, c, nrm, p, org.has_so, o, srec + at, kFaceSlice);
+        sidx[at] = (short)tid;
+      }
+    }
+    float acc[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) acc[q] = 0.f;
+    for (int l0 = 0; l0 < L && ns > 0; l0 += kFaceSlice) {
+      int nl;
+      {
+        const int l = l0 + tid;
+        const bool vis = l < L && (mrows[(size_t)(S + l) * sc.nch + ch] & bit);
+        const int at = block_slot(vis, counts[1], &nl);
+        if (vis) {
+          const fv3 p = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
+          const fv3 o = org.has_lo ? mkv(org.lo.at(b, l, 0), org.lo.at(b, l, 1), org.lo.at(b, l, 2))
+                                   : mkv(0.f, 0.f, 0.f);
+          exh_point_record(v, c, nrm, p, org.has_lo, o, lrec + at, kFaceSlice);
+          lidx[at] = (short)tid;
+        }
+      }
+      __syncthreads();
+      const int pairs = ns * nl;
+      // pair index tid + 256 t walks (si, li) with li fastest
+      int si = nl > 0 ? tid / nl : 0, li = nl > 0 ? tid - si * nl : 0;
+      const int dq = nl > 0 ? 256 / nl : 0, dr = nl > 0 ? 256 - dq * nl : 0;
+      for (int pi = tid; pi < pairs; pi += 256) {
+        const float* rs = srec + si;
+        const float* rl = lrec + li;
+        const int s = s0 + sidx[si], l = l0 + lidx[li];
+        li += dr;
+        si += dq;
+        if (li >= nl) {
+          li -= nl;
+          ++si;
+        }
+        const float as = rs[kRecA * kFaceSlice], al = rl[kRecA * kFaceSlice];
+        const float alpha = kf * as * al;
+        if (!(alpha > 0.f)) continue;
+        float d[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+          d[m] = xadd(rs[(kRecD + m) * kFaceSlice], rl[(kRecD + m) * kFaceSlice]);
+        // the vertex order of exh_sort (stable compare-swaps on the path length)
+        int p0 = 0, p1 = 1, p2 = 2;
+        float d0 = d[0], d1 = d[1], d2 = d[2];
+        if (d0 > d1) { float t = d0; d0 = d1; d1 = t; int u = p0; p0 = p1; p1 = u; }
+        if (d1 > d2) { float t = d1; d1 = d2; d2 = t; int u = p1; p1 = p2; p2 = u; }
+        if (d0 > d1) { float t = d0; d0 = d1; d1 = t; int u = p0; p0 = p1; p1 = u; }
+        const float ods = rs[kRecOd * kFaceSlice], odl = rl[kRecOd * kFaceSlice];
+        const float od = xadd(ods, odl);
+        int bin[3];
+        bin[0] = bin_of(xdiv(xsub(xadd(d0, od), bo), bw));
+        bin[1] = bin_of(xdiv(xsub(xadd(d1, od), bo), bw));
+        bin[2] = bin_of(xdiv(xsub(xadd(d2, od), bo), bw));
+        if (bin[0] >= T || bin[2] < 0) continue;
+        const float* col = tgb + (size_t)s * L + l;
+        fv3 da[3];
+        {
+          const fv3 w = wf + mkv(rs[kRecWv * kFaceSlice], rs[(kRecWv + 1) * kFaceSlice],
+                                 rs[(kRecWv + 2) * kFaceSlice]) +
+                        mkv(rl[kRecWv * kFaceSlice], rl[(kRecWv + 1) * kFaceSlice],
+                            rl[(kRecWv + 2) * kFaceSlice]);
+          const fv3 cm = mkv(rs[kRecCm * kFaceSlice] + rl[kRecCm * kFaceSlice],
+                             rs[(kRecCm + 1) * kFaceSlice] + rl[(kRecCm + 1) * kFaceSlice],
+                             rs[(kRecCm + 2) * kFaceSlice] + rl[(kRecCm + 2) * kFaceSlice]);
+          const fv3 g1 = cross(e2, w), g2 = cross(w, e1);
+          da[0] = alpha * (cm - g1 - g2);
+          da[1] = alpha * (cm + g1);
+          da[2] = alpha * (cm + g2);
+        }
+        const float dadm = vdiv(alpha, rho);
+        if (bin[0] == bin[2]) {
+          const float g = __ldg(col + (int64_t)bin[0] * stride);
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            acc[3 * m] += g * da[m].x;
+            acc[3 * m + 1] += g * da[m].y;
+            acc[3 * m + 2] += g * da[m].z;
+          }
+          acc[9] += g * dadm;
+          continue;
+        }
+        // double-float path lengths of the three vertices, then the corners
+        // of the sorted ones relative to bin[0]
+        const DFloat odf = df_add(DFloat{ods, rs[kRecOdlo * kFaceSlice]},
+                                  DFloat{odl, rl[kRecOdlo * kFaceSlice]});
+        float xo[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          const DFloat path =
+              df_add(df_add(DFloat{rs[(kRecD + m) * kFaceSlice], rs[(kRecDlo + m) * kFaceSlice]},
+                            DFloat{rl[(kRecD + m) * kFaceSlice], rl[(kRecDlo + m) * kFaceSlice]}),
+                     odf);
+          xo[m] = bin_offset(path, bo, bw, inv_bw, bin[0]);
+        }
+        auto pick = [](const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); };
+        const float x[3] = {pick(xo, p0), pick(xo, p1), pick(xo, p2)};
+        TentGrad tgr;
+        tent_grad(col, stride, T, x, bin, tgr);
+        const float span = x[2] - x[0];
+        const float kk = vdiv(-2.f, bw * span * span);
+        // tent terms per sorted position: gamma_k u_(perm k), u = u_s + u_l
+        const float gs0 = vdiv(tgr.a0, bw) - tgr.ayc * kk, gs1 = vdiv(tgr.a1, bw);
+        const float gs2 = vdiv(tgr.a2, bw) + tgr.ayc * kk;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          const float gm = m == p0 ? gs0 : (m == p1 ? gs1 : gs2);
+          const float ag = alpha * gm;
+          const fv3 u = mkv(rs[(kRecU + 3 * m) * kFaceSlice] + rl[(kRecU + 3 * m) * kFaceSlice],
+                            rs[(kRecU + 3 * m + 1) * kFaceSlice] +
+                                rl[(kRecU + 3 * m + 1) * kFaceSlice],
+                            rs[(kRecU + 3 * m + 2) * kFaceSlice] +
+                                rl[(kRecU + 3 * m + 2) * kFaceSlice]);
+          acc[3 * m] += tgr.part0 * da[m].x + ag * u.x;
+          acc[3 * m + 1] += tgr.part0 * da[m].y + ag * u.y;
+          acc[3 * m + 2] += tgr.part0 * da[m].z + ag * u.z;
+        }
+        acc[9] += dadm * tgr.part0;
+      }
+      __syncthreads();  // records are rewritten for the next laser chunk / face
+    }
+    // the face's gradient: warp sums, then one thread per vertex component
+#pragma unroll
+    for (int q = 0; q < 10; ++q) {
+      const float t = warp_sum(acc[q]);
+      if (lane == 0) red[warp][q] = t;
+    }
+    __syncthreads();
+    if (tid < 10 && ns > 0) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w][tid];
+      const int vi[3] = {__float_as_int(s1r.w), __float_as_int(s2r.w), __float_as_int(s3r.w)};
+      if (tid < 9) {
+        const int m = tid / 3, a = tid - 3 * m;
+        if (vi[m] < 0 || vi[m] >= out.V) {
+          atomicOr(sc.status, kStatusFaceIndexRange);
+        } else if (out.vg) {
+          atomicAdd(out.vg + b * out.vsb + vi[m] * out.vsv + a * out.vsc, t);
+        }
+      } else if (out.mg) {
+        for (int m = 0; m < 3; ++m)
+          if (vi[m] >= 0 && vi[m] < out.V)
+            atomicAdd(out.mg + b * out.msb + vi[m] * out.msv, (1.f / 3.f) * t);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <int LT>
 static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
                             const Origins& org, int S, int L, float* out, int T, float bw,
@@ -543,9 +825,23 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   const int split =
       tune::grad_split("mesh.exhaustive.grad.split", (int64_t)sc.nch * sc.B, S, kMaxSlice);
   const int64_t slice = ceil_div(S, split);
-  // Compacted by default (14.7 s against 17.7 s for per-lane mask tests on the
-  // 32-mesh batch); "mesh.exhaustive.grad.mode" = 1 selects the latter.
-  if (tune::get("mesh.exhaustive.grad.mode") == 1) {
+  // Separable point records (exh_grad_face_kernel) by default;
+  // "mesh.exhaustive.grad.mode" = 1 selects per-lane mask tests and 2 the
+  // compacted triples (14.7 s against 17.7 s for per-lane mask tests on the
+  // 32-mesh batch).
+  const int mode = tune::get("mesh.exhaustive.grad.mode");
+  if (mode != 1 && mode != 2) {
+    const size_t smem = sizeof(float) * 2 * kRec * kFaceSlice;
+    TOTRI_CUDA(tune::ensure_dynamic_smem(reinterpret_cast<const void*>(exh_grad_face_kernel),
+                                         smem));
+    const dim3 grid((unsigned)ceil_div(sc.F, kFacesPerCta), (unsigned)sc.B,
+                    (unsigned)ceil_div(S, kFaceSlice));
+    TOTRI_KERNEL("mesh exhaustive grad", stream,
+                 exh_grad_face_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T,
+                                                                   bw, bo, out));
+    return TOTRI_OK;
+  }
+  if (mode == 1) {
     const size_t smem = sizeof(uint32_t) * (size_t)(S + L);
     if (smem > 200 * 1024)
       return fail(TOTRI_ERR_UNSUPPORTED, "too many wall points for one tile");

@@ -1,5 +1,8 @@
 // Launch counting and optional per-kernel event timing.
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -44,6 +47,16 @@ cudaEvent_t take_event() {
 }  // namespace
 
 bool enabled() { return g_on.load(std::memory_order_relaxed); }
+
+bool nvtx_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("TOTRI_NVTX");
+    return v && v[0] && std::strcmp(v, "0") != 0;
+  }();
+  return on;
+}
+void nvtx_push(const char* name) { nvtxRangePushA(name); }
+void nvtx_pop() { nvtxRangePop(); }
 
 void begin(const char* name, cudaStream_t stream, cudaEvent_t* start) {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -3,10 +3,12 @@
 // Reference: src/util/rbf2volume_cuda.cu (:50-93 forward, one thread per voxel
 // reading every Gaussian from global memory; :124-201 gradient, one block
 // column per Gaussian with a shared-memory tree reduction and an atomic per
-// (Gaussian, channel, 64 voxels)). Here the forward stages Gaussians in shared
-// memory tiles; the gradient gives each thread one Gaussian and a chunk of
-// voxels staged in shared memory, accumulates all 4+A channels in registers
-// and issues 4+A atomics per (Gaussian, chunk).
+// (Gaussian, channel, 64 voxels)). Here both kernels work on bricks of voxels
+// and take the Gaussians in shared-memory tiles, skipping those that
+// contribute exactly zero to the whole brick (the underflow cull below): the
+// forward gives each thread one voxel; the gradient gives each surviving
+// Gaussian a warp over the brick's voxels, accumulates all 4+A channels in
+// registers and issues 4+A atomics per (Gaussian, brick).
 #include <algorithm>
 #include <string>
 
@@ -42,37 +44,106 @@ __device__ __forceinline__ float exp2_approx(float x) {
 
 constexpr float kLog2e = 1.4426950408889634f;
 
+__device__ __forceinline__ float warp_sum_f(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
 struct Rbf {  // [B, N, C] with strides
   const float* p;
   int64_t sb, sn, sc;
   __device__ float at(int b, int i, int c) const { return p[b * sb + i * sn + c * sc]; }
 };
 
-__global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int N, int C,
+// Tile-level cull at the underflow radius. ex2.approx.ftz flushes results
+// below 2^-126 to zero, so a Gaussian whose exponent argument d2 * k2 lies
+// below -126.5 at every voxel of a brick adds exactly +0 (or -0) there, and
+// an accumulator that started at +0 is unchanged by it: skipping it leaves the
+// sums bit for bit the same, in the same order. The test uses the squared
+// distance from the centre to the brick's coordinate box (voxel coordinates
+// are monotone in the index), computed in FP32, against 128 / |k2|, which
+// leaves a margin far beyond the few ulps of the voxel-level arithmetic.
+// Gaussians with a non-finite value are never culled (0 * inf would not be a
+// zero term). The tuning key "rbf.cull" = 1 turns the cull off.
+constexpr float kCullArg = 128.f;
+
+// Squared distance from (cx, cy, cz) to the box [lo, hi].
+__device__ __forceinline__ float box_dist2(float cx, float cy, float cz, const float lo[3],
+                                           const float hi[3]) {
+  const float dx = fmaxf(fmaxf(lo[0] - cx, cx - hi[0]), 0.f);
+  const float dy = fmaxf(fmaxf(lo[1] - cy, cy - hi[1]), 0.f);
+  const float dz = fmaxf(fmaxf(lo[2] - cz, cz - hi[2]), 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// Coordinate box of the voxels [i0, i1] of one axis.
+__device__ __forceinline__ void axis_box(float s, float e, int n, int i0, int i1, float& lo,
+                                         float& hi) {
+  const float a = coord(s, e, n, i0), b = coord(s, e, n, i1);
+  lo = fminf(a, b);
+  hi = fmaxf(a, b);
+}
+
+// Block-wide compaction: this thread's slot among the flagged threads (or -1);
+// *total receives their count. All threads of the block call it.
+__device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned bal = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) warp_counts[warp] = __popc(bal);
+  __syncthreads();
+  int base = 0, sum = 0;
+  for (int w = 0; w < nw; ++w) {
+    const int c = warp_counts[w];
+    base += w < warp ? c : 0;
+    sum += c;
+  }
+  *total = sum;
+  return flag ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
+}
+
+// Forward: a CTA per brick of 8 x 8 x 4 voxels (x fastest), one thread per
+// voxel; Gaussians come in tiles of 256, each culled against the brick's box,
+// and the survivors are evaluated in their original order.
+__global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int N, int C, int cull,
                                                       float* __restrict__ vol) {
   __shared__ float tile[kTile][4 + kMaxAttr];
+  __shared__ int counts[8];
   const int A = C - 4;
   const int64_t nv = (int64_t)g.D * g.H * g.W;
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int xi = (int)(v % g.W), yi = (int)((v / g.W) % g.H), zi = (int)(v / ((int64_t)g.W * g.H));
+  const int tid = threadIdx.x;
+  const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 4;
+  const int xi = bx + (tid & 7), yi = by + ((tid >> 3) & 7), zi = bz + (tid >> 6);
+  const bool inside = xi < g.W && yi < g.H && zi < g.D;
   const float x = coord(g.sx, g.ex, g.W, xi), y = coord(g.sy, g.ey, g.H, yi);
   const float z = coord(g.sz, g.ez, g.D, zi);
+  float lo[3], hi[3];
+  axis_box(g.sx, g.ex, g.W, bx, min(bx + 7, g.W - 1), lo[0], hi[0]);
+  axis_box(g.sy, g.ey, g.H, by, min(by + 7, g.H - 1), lo[1], hi[1]);
+  axis_box(g.sz, g.ez, g.D, bz, min(bz + 3, g.D - 1), lo[2], hi[2]);
   float sum = 0.f;
   float attr[kMaxAttr];
 #pragma unroll
   for (int a = 0; a < kMaxAttr; ++a) attr[a] = 0.f;
   for (int i0 = 0; i0 < N; i0 += kTile) {
-    __syncthreads();
-    for (int j = threadIdx.x; j < kTile * C; j += blockDim.x) {
-      const int i = j / C, c = j - i * C;
-      if (i0 + i < N) {
-        const float val = r.at(b, i0 + i, c);
-        // slot 3 holds -log2(e) / (2 sigma^2) instead of sigma
-        tile[i][c] = c == 3 ? -0.5f * kLog2e / (val * val) : val;
+    __syncthreads();  // the previous tile has been read
+    float val[4 + kMaxAttr];
+    bool keep = false;
+    if (i0 + tid < N) {
+      bool finite = true;
+      for (int c = 0; c < C; ++c) {
+        val[c] = r.at(b, i0 + tid, c);
+        finite = finite && isfinite(val[c]);
       }
+      // slot 3 holds -log2(e) / (2 sigma^2) instead of sigma
+      val[3] = -0.5f * kLog2e / (val[3] * val[3]);
+      keep = !cull || !finite || !isfinite(val[3]) ||
+             !(box_dist2(val[0], val[1], val[2], lo, hi) * -val[3] > kCullArg);
     }
+    int cnt;
+    const int at = block_slot(keep, counts, &cnt);
+    if (keep)
+      for (int c = 0; c < C; ++c) tile[at][c] = val[c];
     __syncthreads();
-    const int cnt = min(kTile, N - i0);
     for (int i = 0; i < cnt; ++i) {
       const float dx = tile[i][0] - x, dy = tile[i][1] - y, dz = tile[i][2] - z;
       const float w = exp2_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * tile[i][3]);
@@ -82,7 +153,8 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
         if (a < A) attr[a] += w * tile[i][4 + a];
     }
   }
-  if (v >= nv) return;
+  if (!inside) return;
+  const int64_t v = ((int64_t)zi * g.H + yi) * g.W + xi;
   float* out = vol + (size_t)b * (1 + A) * nv;
   out[v] = sum;
   const float norm = sum < 1e-8f ? 1.f : sum;
@@ -91,102 +163,124 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
     if (a < A) out[(size_t)(1 + a) * nv + v] = attr[a] / norm;
 }
 
-constexpr int kChunk = 512;  // voxels staged per pass
+constexpr int kChunk = 512;  // voxels of a gradient brick (8 x 8 x 8)
 
-// Gradient (rbf2volume_cuda.cu:124-201): thread = Gaussian, CTA = chunk of
-// voxels (coordinates, volume and volume_grad channels staged in shared memory).
-__global__ void __launch_bounds__(128) grad_kernel(Grid g, int b, Rbf r, int N, int C,
+// Gradient (rbf2volume_cuda.cu:124-201): a CTA per brick of 8 x 8 x 8 voxels,
+// whose coordinates, volume and volume_grad channels are staged in shared
+// memory. Gaussians come in tiles of 256, culled against the brick's box as
+// in the forward; each surviving Gaussian goes to one warp, whose lanes take
+// the brick's voxels, accumulate all 4+A channels, reduce them across the
+// warp and add them to rbf_grad with one atomic per channel.
+__global__ void __launch_bounds__(256) grad_kernel(Grid g, int b, Rbf r, int N, int C, int cull,
                                                    const float* __restrict__ vol,
                                                    const float* __restrict__ vgrad,
                                                    float* __restrict__ rgrad, int64_t gsb,
-                                                   int64_t gsn, int64_t gsc, int64_t vox_per_cta) {
-  extern __shared__ float sm[];  // [kChunk][4 + 2 * (1 + A)] : x y z pad | vol[1+A] | grad[1+A]
+                                                   int64_t gsn, int64_t gsc) {
+  extern __shared__ float sm[];  // [kChunk][4 + 2 * (1 + A)] : x y z valid | vol[1+A] | grad[1+A]
+  __shared__ int list[kTile];
+  __shared__ int counts[8];
   const int A = C - 4;
   const int stride = 4 + 2 * (1 + A);
   const int64_t nv = (int64_t)g.D * g.H * g.W;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = i < N;
-  float xr = 0.f, yr = 0.f, zr = 0.f, sigma = 1.f;
-  float ra[kMaxAttr];
-#pragma unroll
-  for (int a = 0; a < kMaxAttr; ++a) ra[a] = 0.f;
-  if (active) {
-    xr = r.at(b, i, 0);
-    yr = r.at(b, i, 1);
-    zr = r.at(b, i, 2);
-    sigma = r.at(b, i, 3);
-#pragma unroll
-    for (int a = 0; a < kMaxAttr; ++a)
-      if (a < A) ra[a] = r.at(b, i, 4 + a);
-  }
-  const float is2 = 1.f / (sigma * sigma);
-  const float k2 = -0.5f * kLog2e * is2;  // w = 2^(d2 * k2)
-  const float is3 = is2 / sigma;
-  float gx = 0.f, gy = 0.f, gz = 0.f, gs = 0.f;
-  float ga[kMaxAttr];
-#pragma unroll
-  for (int a = 0; a < kMaxAttr; ++a) ga[a] = 0.f;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 8;
   const float* vb = vol + (size_t)b * (1 + A) * nv;
   const float* gb = vgrad + (size_t)b * (1 + A) * nv;
-  const int64_t v_begin = (int64_t)blockIdx.y * vox_per_cta;
-  const int64_t v_end = min(nv, v_begin + vox_per_cta);
-  for (int64_t c0 = v_begin; c0 < v_end; c0 += kChunk) {
-    const int cnt = (int)min((int64_t)kChunk, v_end - c0);
-    __syncthreads();
-    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      const int64_t v = c0 + j;
-      const int xi = (int)(v % g.W), yi = (int)((v / g.W) % g.H), zi = (int)(v / ((int64_t)g.W * g.H));
-      float* e = sm + j * stride;
-      e[0] = coord(g.sx, g.ex, g.W, xi);
-      e[1] = coord(g.sy, g.ey, g.H, yi);
-      e[2] = coord(g.sz, g.ez, g.D, zi);
-      for (int q = 0; q <= A; ++q) {
-        e[4 + q] = vb[(size_t)q * nv + v];
-        e[4 + 1 + A + q] = gb[(size_t)q * nv + v];
-      }
-    }
-    __syncthreads();
-    if (!active) continue;
-    for (int j = 0; j < cnt; ++j) {
-      const float* e = sm + j * stride;
-      const float x = e[0], y = e[1], z = e[2];
-      const float ex = x - xr, ey = y - yr, ez = z - zr;
-      const float d2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-      const float w = exp2_approx(d2 * k2);
-      const float wi = is2 * w;
-      const float dwx = ex * wi, dwy = ey * wi, dwz = ez * wi;
-      const float dws = d2 * is3 * w;
-      float dl = e[4 + 1 + A];
-      if (A > 0) {
-        float v0 = e[4];
-        if (v0 < 1e-8f) v0 = 1.f;
-        const float inv = 1.f / v0;
-        float sum = 0.f;
-#pragma unroll
-        for (int a = 0; a < kMaxAttr; ++a) {
-          if (a < A) {
-            const float dla = e[4 + 1 + A + 1 + a];
-            sum += dla * (ra[a] - e[4 + 1 + a]);
-            ga[a] += dla * w * inv;
-          }
-        }
-        dl += sum * inv;
-      }
-      gx += dwx * dl;
-      gy += dwy * dl;
-      gz += dwz * dl;
-      gs += dws * dl;
+  for (int j = tid; j < kChunk; j += blockDim.x) {
+    const int xi = bx + (j & 7), yi = by + ((j >> 3) & 7), zi = bz + (j >> 6);
+    float* e = sm + j * stride;
+    const bool in = xi < g.W && yi < g.H && zi < g.D;
+    e[0] = coord(g.sx, g.ex, g.W, xi);
+    e[1] = coord(g.sy, g.ey, g.H, yi);
+    e[2] = coord(g.sz, g.ez, g.D, zi);
+    e[3] = in ? 1.f : 0.f;
+    const int64_t v = in ? ((int64_t)zi * g.H + yi) * g.W + xi : 0;
+    for (int q = 0; q <= A; ++q) {
+      e[4 + q] = in ? vb[(size_t)q * nv + v] : 0.f;
+      e[4 + 1 + A + q] = in ? gb[(size_t)q * nv + v] : 0.f;
     }
   }
-  if (!active) return;
-  float* out = rgrad + b * gsb + i * gsn;
-  atomicAdd(out, gx);
-  atomicAdd(out + gsc, gy);
-  atomicAdd(out + 2 * gsc, gz);
-  atomicAdd(out + 3 * gsc, gs);
+  float lo[3], hi[3];
+  axis_box(g.sx, g.ex, g.W, bx, min(bx + 7, g.W - 1), lo[0], hi[0]);
+  axis_box(g.sy, g.ey, g.H, by, min(by + 7, g.H - 1), lo[1], hi[1]);
+  axis_box(g.sz, g.ez, g.D, bz, min(bz + 7, g.D - 1), lo[2], hi[2]);
+  for (int i0 = 0; i0 < N; i0 += kTile) {
+    __syncthreads();  // the staged voxels are written / the previous list is read
+    bool keep = false;
+    if (i0 + tid < N) {
+      const float cx = r.at(b, i0 + tid, 0), cy = r.at(b, i0 + tid, 1);
+      const float cz = r.at(b, i0 + tid, 2), sg = r.at(b, i0 + tid, 3);
+      const float k2 = -0.5f * kLog2e * (1.f / (sg * sg));
+      keep = !cull || !(isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(k2)) ||
+             !(box_dist2(cx, cy, cz, lo, hi) * -k2 > kCullArg);
+    }
+    int cnt;
+    const int at = block_slot(keep, counts, &cnt);
+    if (keep) list[at] = i0 + tid;
+    __syncthreads();
+    for (int q = warp; q < cnt; q += 8) {
+      const int i = list[q];
+      const float xr = r.at(b, i, 0), yr = r.at(b, i, 1), zr = r.at(b, i, 2);
+      const float sigma = r.at(b, i, 3);
+      float ra[kMaxAttr];
 #pragma unroll
-  for (int a = 0; a < kMaxAttr; ++a)
-    if (a < A) atomicAdd(out + (4 + a) * gsc, ga[a]);
+      for (int a = 0; a < kMaxAttr; ++a) ra[a] = a < A ? r.at(b, i, 4 + a) : 0.f;
+      const float is2 = 1.f / (sigma * sigma);
+      const float k2 = -0.5f * kLog2e * is2;  // w = 2^(d2 * k2)
+      const float is3 = is2 / sigma;
+      float gx = 0.f, gy = 0.f, gz = 0.f, gs = 0.f;
+      float ga[kMaxAttr];
+#pragma unroll
+      for (int a = 0; a < kMaxAttr; ++a) ga[a] = 0.f;
+      for (int j = lane; j < kChunk; j += 32) {
+        const float* e = sm + j * stride;
+        if (e[3] == 0.f) continue;  // outside the grid
+        const float ex = e[0] - xr, ey = e[1] - yr, ez = e[2] - zr;
+        const float d2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+        const float w = exp2_approx(d2 * k2);
+        const float wi = is2 * w;
+        const float dwx = ex * wi, dwy = ey * wi, dwz = ez * wi;
+        const float dws = d2 * is3 * w;
+        float dl = e[4 + 1 + A];
+        if (A > 0) {
+          float v0 = e[4];
+          if (v0 < 1e-8f) v0 = 1.f;
+          const float inv = 1.f / v0;
+          float s = 0.f;
+#pragma unroll
+          for (int a = 0; a < kMaxAttr; ++a) {
+            if (a < A) {
+              const float dla = e[4 + 1 + A + 1 + a];
+              s += dla * (ra[a] - e[4 + 1 + a]);
+              ga[a] += dla * w * inv;
+            }
+          }
+          dl += s * inv;
+        }
+        gx += dwx * dl;
+        gy += dwy * dl;
+        gz += dwz * dl;
+        gs += dws * dl;
+      }
+      gx = warp_sum_f(gx);
+      gy = warp_sum_f(gy);
+      gz = warp_sum_f(gz);
+      gs = warp_sum_f(gs);
+#pragma unroll
+      for (int a = 0; a < kMaxAttr; ++a)
+        if (a < A) ga[a] = warp_sum_f(ga[a]);
+      if (lane == 0) {
+        float* out = rgrad + b * gsb + i * gsn;
+        atomicAdd(out, gx);
+        atomicAdd(out + gsc, gy);
+        atomicAdd(out + 2 * gsc, gz);
+        atomicAdd(out + 3 * gsc, gs);
+#pragma unroll
+        for (int a = 0; a < kMaxAttr; ++a)
+          if (a < A) atomicAdd(out + (4 + a) * gsc, ga[a]);
+      }
+    }
+  }
 }
 
 }  // namespace rbf
@@ -230,10 +324,12 @@ int totri_rbf2volume_gaussian_forward(const totri_array_t* r, const totri_array_
   TOTRI_TRY(check_rbf(r, vol, g, rr, B, N, C, start, end));
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   if (nv == 0 || B == 0) return TOTRI_OK;
+  const int cull = tune::get("rbf.cull") != 1;
+  const dim3 grid((unsigned)ceil_div(g.W, 8), (unsigned)ceil_div(g.H, 8), (unsigned)ceil_div(g.D, 4));
   for (int b = 0; b < (int)B; ++b)
     TOTRI_KERNEL("rbf2volume forward", stream,
-                 rbf::forward_kernel<<<(unsigned)ceil_div(nv, 256), 256, 0, stream>>>(
-                     g, b, rr, (int)N, C, static_cast<float*>(vol->data)));
+                 rbf::forward_kernel<<<grid, 256, 0, stream>>>(g, b, rr, (int)N, C, cull,
+                                                               static_cast<float*>(vol->data)));
   return TOTRI_OK;
 }
 
@@ -261,19 +357,14 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* r, const totri_array_t* 
   const size_t smem = sizeof(float) * rbf::kChunk * (4 + 2 * (1 + A));
   TOTRI_CUDA(tune::ensure_dynamic_smem(
       reinterpret_cast<const void*>(rbf::grad_kernel), smem));
-  // voxels per CTA: enough CTAs to fill the GPU several times over
-  const int64_t rbf_blocks = ceil_div(N, 128);
-  int64_t chunks = std::max<int64_t>(1, (152 * 8 + rbf_blocks - 1) / rbf_blocks);
-  chunks = std::min<int64_t>(chunks, ceil_div(nv, rbf::kChunk));
-  const int64_t per = ceil_div(ceil_div(nv, chunks), rbf::kChunk) * rbf::kChunk;
-  chunks = ceil_div(nv, per);
+  const int cull = tune::get("rbf.cull") != 1;
+  const dim3 grid((unsigned)ceil_div(g.W, 8), (unsigned)ceil_div(g.H, 8), (unsigned)ceil_div(g.D, 8));
   for (int b = 0; b < (int)B; ++b)
     TOTRI_KERNEL("rbf2volume grad", stream,
-                 rbf::grad_kernel<<<dim3((unsigned)rbf_blocks, (unsigned)chunks), 128, smem,
-                                    stream>>>(
-                     g, b, rr, (int)N, C, static_cast<const float*>(vol->data),
+                 rbf::grad_kernel<<<grid, 256, smem, stream>>>(
+                     g, b, rr, (int)N, C, cull, static_cast<const float*>(vol->data),
                      static_cast<const float*>(vgrad->data), static_cast<float*>(rgrad->data),
-                     rgrad->strides[0], rgrad->strides[1], rgrad->strides[2], per));
+                     rgrad->strides[0], rgrad->strides[1], rgrad->strides[2]));
   return TOTRI_OK;
 }
 

@@ -4,6 +4,8 @@
 //   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
 //   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk
 //   "mesh.visibility.queue"     1: queued BVH searches (visibility_queue_kernel)
+//   "mesh.visibility.wide"      2: binary BVH search after the surface-walk prefix
+//                               (the default is the 4-wide search)
 //   "mesh.confocal.grad.split"  scan-point slices per confocal gradient chunk
 //   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
 #pragma once

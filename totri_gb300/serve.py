@@ -11,11 +11,19 @@ Resident state (device memory, kept across requests):
     needs them and kept in an LRU cache (bins do not change visibility).
 
 Requests are admitted first-come-first-served with a bounded look-ahead
-whenever a stream slot is free and their device memory (outputs, scratch,
-masks still to be computed) fits the HBM budget next to the resident state;
-admitted requests run concurrently on separate CUDA streams, so small requests
-overlap each other and large ones. A request's result is copied to pinned host
-memory on its stream and its future resolves when that copy has completed.
+whenever a stream slot of their class is free and their device memory
+(outputs, scratch, masks still to be computed) fits the HBM budget next to the
+resident state; admitted requests run concurrently on separate CUDA streams.
+Each request gets a rough GPU-time estimate (``Server.cost_ms``): small
+requests run on high-priority streams, large ones (estimated at
+``large_ms`` or more: big backprojections, first renders of a large mesh on a
+large grid) on normal-priority streams, so the thread blocks of a small
+request are dispatched ahead of the blocks a large kernel still has queued
+and a small request does not wait for a large one to finish. A request's
+result is copied to pinned host memory on its stream and its future resolves
+when that copy has completed. Cancelling a future drops a queued request; an
+admitted request runs to the end on the GPU, its result is discarded and its
+memory returns to the budget when it completes.
 
 Kinds (``Request.kind``):
   * "render"      — confocal mesh transient [T, S] (``mesh``, ``grid``, ``bins``);
@@ -59,6 +67,7 @@ class Request:
     arrival: float = 0.0
     admitted: float = 0.0
     done: float = 0.0
+    large: bool = False
 
 
 class Budget:
@@ -136,9 +145,12 @@ class _Mesh:
 
 
 class Server:
-    """Continuous-batching request server (one GPU, `slots` CUDA streams)."""
+    """Continuous-batching request server (one GPU): `slots` high-priority CUDA
+    streams for small requests and `large_slots` normal-priority streams for
+    requests estimated at `large_ms` or more."""
 
-    def __init__(self, device=None, hbm_budget=80e9, slots=4, lookahead=8):
+    def __init__(self, device=None, hbm_budget=80e9, slots=4, lookahead=8, large_slots=2,
+                 large_ms=5.0):
         device = torch.device(device or "cuda")
         if device.index is None:
             device = torch.device("cuda", torch.cuda.current_device())
@@ -147,7 +159,11 @@ class Server:
         self.budget = Budget(hbm_budget)
         self.masks = MaskCache(self.budget)
         self.meshes, self.grids, self.measurements = {}, {}, {}
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.streams = ([torch.cuda.Stream(self.device, priority=hi) for _ in range(slots)] +
+                        [torch.cuda.Stream(self.device, priority=lo) for _ in range(large_slots)])
+        self.slot_large = [False] * slots + [True] * large_slots
+        self.large_ms = large_ms
         self.lookahead = lookahead
         self.queue = collections.deque()
         self.inflight = {}  # slot -> (request, future, event, release, result)
@@ -156,6 +172,7 @@ class Server:
         self.thread = None
         self.running = False
         self.completed = []
+        self.cancelled = 0  # requests cancelled while in flight
 
     # -- resident state -----------------------------------------------------
 
@@ -234,6 +251,36 @@ class Server:
             raise ValueError("backproject requests need a VolumeDef")
         if r.kind not in ("render", "grad", "backproject", "fit_pose"):
             raise ValueError("unknown request kind %r" % r.kind)
+
+    # Rates behind cost_ms, measured on one GB300 (the differentiable
+    # 20,480-face workload and the 128^3 Velten backprojection): visibility
+    # 9e9 (point, face) pairs/s, splat 1.1e11, gradient 6.5e10, backprojection
+    # 9e11 voxel-point pairs/s, device-to-host copies 25 GB/s.
+    _RATES = dict(visibility=9e9, splat=1.1e11, grad=6.5e10, backproject=9e11, copy=25e9)
+
+    def cost_ms(self, r):
+        """Rough GPU time of request r in ms; it only sorts requests into small
+        and large."""
+        k = self._RATES
+        S = self.grids[r.grid].shape[1]
+        if r.kind == "backproject":
+            vox = 1
+            for n in r.volume.resolution:
+                vox *= int(n)
+            return 1e3 * (vox * S / k["backproject"] + 4 * vox / k["copy"])
+        m = self.meshes[r.mesh]
+        pairs = m.F * S
+        if r.kind == "fit_pose":
+            return 1e3 * r.iterations * pairs * (1 / k["visibility"] + 1 / k["splat"] +
+                                                 1 / k["grad"])
+        sec = pairs / k["splat"]
+        if r.kind == "grad":
+            sec += pairs / k["grad"] + 4 * 4 * m.verts.shape[1] / k["copy"]
+        else:
+            sec += 4 * r.bins.num * S / k["copy"]
+        if self.masks.get((r.mesh, r.grid)) is None:
+            sec += pairs / k["visibility"]
+        return 1e3 * sec
 
     def _mask_bytes(self, r):
         S = self.grids[r.grid].shape[1]
@@ -345,7 +392,8 @@ class Server:
         return out
 
     def _admit_one(self):
-        """Admits the first of the next `lookahead` queued requests that fits."""
+        """Admits the first of the next `lookahead` queued requests that fits
+        and has a free stream of its class; drops cancelled ones."""
         free = [i for i in range(len(self.streams)) if i not in self.inflight]
         if not free or not self.queue:
             return False
@@ -353,6 +401,13 @@ class Server:
         ceiling = self.budget.total - (self.budget.resident - cached)
         for qi in range(min(self.lookahead, len(self.queue))):
             r, fut = self.queue[qi]
+            if fut.cancelled():
+                del self.queue[qi]
+                return True
+            large = self.cost_ms(r) >= self.large_ms
+            slots = [i for i in free if self.slot_large[i] == large]
+            if not slots:
+                continue
             need = self._need(r)
             if need > ceiling:  # could never fit, even on an idle device
                 del self.queue[qi]
@@ -363,8 +418,9 @@ class Server:
             if not self.budget.fits(need) and not self.masks.make_room(need):
                 continue
             del self.queue[qi]
-            slot = free[0]
+            slot = slots[0]
             stream = self.streams[slot]
+            r.large = large
             key = (r.mesh, r.grid) if r.kind in ("render", "grad") else None
             new_mask = key is not None and key not in self.masks.entries
             self.budget.take(need)
@@ -403,8 +459,11 @@ class Server:
             if r.kind in ("render", "grad"):
                 self.masks.unpin((r.mesh, r.grid))
             r.done = time.perf_counter()
-            self.completed.append(r)
-            fut.set_result(result)
+            if fut.cancelled():  # cancelled in flight: the result is dropped
+                self.cancelled += 1
+            else:
+                self.completed.append(r)
+                fut.set_result(result)
             done = True
         return done
 
@@ -460,13 +519,31 @@ class Server:
     def __exit__(self, *exc):
         self.stop()
 
-    def latency_ms(self):
-        """(p50, p99) of completion - arrival over completed requests, in ms."""
-        lat = sorted(1e3 * (r.done - r.arrival) for r in self.completed)
+    @staticmethod
+    def _p50_p99(values):
+        lat = sorted(values)
         if not lat:
             return None, None
         pick = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
         return pick(0.5), pick(0.99)
+
+    def latency_ms(self):
+        """(p50, p99) of completion - arrival over completed requests, in ms."""
+        return self._p50_p99([1e3 * (r.done - r.arrival) for r in self.completed])
+
+    def latency_breakdown(self):
+        """p50/p99 (ms) of the queue wait (admission - arrival) and the service
+        time (completion - admission), over all completed requests and per
+        class (small / large), with the request counts."""
+        out = {}
+        for name, sel in (("all", lambda r: True), ("small", lambda r: not r.large),
+                          ("large", lambda r: r.large)):
+            rs = [r for r in self.completed if sel(r)]
+            out[name] = {"requests": len(rs),
+                         "latency": self._p50_p99([1e3 * (r.done - r.arrival) for r in rs]),
+                         "wait": self._p50_p99([1e3 * (r.admitted - r.arrival) for r in rs]),
+                         "service": self._p50_p99([1e3 * (r.done - r.admitted) for r in rs])}
+        return out
 
 
 def ctypes_ptr(t):

@@ -24,6 +24,25 @@ def mesh_workspace(B, V, F, P, device):
     return torch.empty(n, dtype=torch.uint8, device=device)
 
 
+# Status bits that report internal errors (a BVH search at its limit, an index
+# read from device data out of range in the bounds-checking build); the face
+# index bit reports an input and is documented behaviour.
+INTERNAL_STATUS = 2 | 4
+
+
+def check_device_status(ws, device):
+    """Bounds-checking build only: synchronises and raises RuntimeError when the
+    call whose workspace is `ws` raised an internal-error status bit."""
+    from .. import build
+    if ws is None or not build.bounds_check():
+        return
+    flags = ctypes.c_uint32(0)
+    _lib.load().totri_mesh_workspace_status(ctypes.c_void_p(ws.data_ptr()), ws.numel(),
+                                            ctypes.byref(flags), _lib.stream_of(device))
+    if flags.value & INTERNAL_STATUS:
+        raise RuntimeError("device status flags 0x%x after a mesh call" % flags.value)
+
+
 def ws_args(ws):
     if ws is None:
         return ctypes.c_void_p(None), 0

@@ -7,7 +7,7 @@ sm_103a kernels of libtotri_gb300.so on the current CUDA stream.
 import torch
 
 from .. import _lib
-from ._common import dense_out, finish_out, mesh_workspace, ws_args
+from ._common import check_device_status, dense_out, finish_out, mesh_workspace, ws_args
 
 
 def _mesh_call(name, tensors, bw, bo, model, points):
@@ -17,6 +17,7 @@ def _mesh_call(name, tensors, bw, bo, model, points):
     st = getattr(lib, name)(*[_lib.array(t) for t in tensors], float(bw), float(bo), int(model),
                             *ws_args(ws), _lib.stream_of(verts.device))
     _lib.check(st)
+    check_device_status(ws, verts.device)
     return ws
 
 
