@@ -136,7 +136,8 @@ def test_velten_bins_exact(cuda_lib, offset, origin):
 def test_velten_tiled_equals_untiled(cuda_lib):
     """The shared-memory tiled Velten kernel sums the same values in the same
     order as the one-voxel-per-thread kernel: identical volumes for 1, 2 and
-    4 voxels per thread, including grids that are not a multiple of the voxel
+    4 voxels per thread, with registers capped (the default) or not
+    ("backprojection.velten.occupancy" = 1), including grids that are not a multiple of the voxel
     block and a scan whose bin windows overflow the staged rows."""
     from totri_gb300 import autotune
     g = np.random.default_rng(5)
@@ -146,9 +147,10 @@ def test_velten_tiled_equals_untiled(cuda_lib):
         sp = torch.from_numpy(np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S),
                                         np.zeros(S)], -1).astype(np.float32))[None].cuda()
         out = []
-        for mode, vz in ((1, 0), (0, 1), (0, 2), (0, 4)):
+        for mode, vz, occ in ((1, 0, 0), (0, 1, 0), (0, 2, 0), (0, 4, 0), (0, 4, 1)):
             autotune.set_tile("backprojection.velten.mode", mode)
             autotune.set_tile("backprojection.velten.vz", vz)
+            autotune.set_tile("backprojection.velten.occupancy", occ)
             v = torch.empty((1,) + res, device="cuda")
             K.backprojection_confocal_velten_forward(tr, sp, torch.empty((1, 0, 3), device="cuda"),
                                                      v, (-0.5, -0.4, 0.5), (0.5, 0.45, 1.5), bw,
@@ -156,5 +158,6 @@ def test_velten_tiled_equals_untiled(cuda_lib):
             out.append(v)
         autotune.set_tile("backprojection.velten.mode", 0)
         autotune.set_tile("backprojection.velten.vz", 0)
+        autotune.set_tile("backprojection.velten.occupancy", 0)
         for o in out[1:]:
             assert torch.equal(out[0], o)

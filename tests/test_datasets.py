@@ -1,6 +1,7 @@
-"""MATLAB-format dataset loaders against the reference's own loaders run on
-the same small files (tests/golden/make_golden_datasets.py), and the Zaragoza
-loader on a synthetic mapping of its datasets."""
+"""Dataset loaders against the reference's own loaders run on the same small
+inputs: the MATLAB formats (tests/golden/make_golden_datasets.py) and the
+HDF5 formats (tests/golden/make_golden_hdf5.py); plus the Zaragoza and Lindell
+layouts checked directly on synthetic arrays."""
 import os
 
 import numpy as np
@@ -94,3 +95,50 @@ def test_lindell_fk2019_arrays():
     assert np.array_equal(ds.transient.numpy(), want)
     assert ds.scan_points.shape == (1, 512, 512, 3)
     assert abs(ds.bin_def.width_s - 32e-12) < 1e-20
+
+
+def _golden_cases(name):
+    z = dict(np.load(os.path.join(HERE, name)))
+    cases = sorted({k.split("_", 1)[0][2:] for k in z if k.startswith("in")})
+    for c in cases:
+        inputs = {k.split("_", 1)[1]: v for k, v in z.items() if k.startswith("in%s_" % c)}
+        outputs = {k.split("_", 1)[1]: v for k, v in z.items() if k.startswith("out%s_" % c)}
+        yield inputs, outputs
+
+
+def test_zaragoza_matches_reference_loader():
+    """Zaragoza against the reference's own loader (totri/data/zaragoza.py:57-128)
+    run on the same datasets (tests/golden/make_golden_hdf5.py): bins, volume
+    box, grid extent, summed transient, wall-frame points, normals and origin,
+    and the rectified transient (its rolls wrap: 2 d / bin width > T)."""
+    from totri_gb300.data import Zaragoza
+    n = 0
+    for m, ref in _golden_cases("zaragoza.npz"):
+        ds = Zaragoza(m)
+        assert np.allclose([ds.bin_def.width, ds.bin_def.offset, ds.bin_def.num], ref["bins"])
+        assert np.allclose([ds.volume_def.start, ds.volume_def.end], ref["volume"])
+        assert tuple(ds.volume_def.resolution) == tuple(ref["resolution"])
+        assert np.allclose(ds.scan_point_extent, ref["extent"])
+        assert np.array_equal(ds.transient.numpy(), ref["transient"])
+        assert np.array_equal(ds.scan_points.numpy(), ref["scan_points"])
+        assert np.array_equal(ds.scan_normals.numpy(), ref["scan_normals"])
+        assert np.array_equal(ds.scan_origin.numpy(), ref["scan_origin"])
+        assert np.array_equal(Zaragoza(m, rectify=True).transient.numpy(), ref["rectified"])
+        assert not np.array_equal(ref["rectified"], ref["transient"])
+        n += 1
+    assert n == 2
+
+
+def test_lindell_fk2019_matches_reference_loader():
+    """LindellFk2019 against the reference's own loader
+    (totri/data/lindellfk2019.py:33-57) on the same arrays: rolled, cropped,
+    flipped transient, the wall grid (every 64th point) and the bins."""
+    from totri_gb300.data import LindellFk2019
+    n = 0
+    for m, ref in _golden_cases("lindellfk2019.npz"):
+        ds = LindellFk2019(m["meas"], m["tofgrid"], crop=int(m["crop"]))
+        assert np.array_equal(ds.transient.numpy(), ref["transient"])
+        assert np.array_equal(ds.scan_points[0, ::64, ::64].numpy(), ref["scan_points_every64"])
+        assert np.allclose([ds.bin_def.width_s, ds.bin_def.offset, ds.bin_def.num], ref["bins"])
+        n += 1
+    assert n == 2

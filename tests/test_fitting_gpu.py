@@ -210,3 +210,150 @@ def test_rbf_fit_moves_add_blobs(cuda_lib):
     _, final = fit.loss_all(out, TransientBackgroundEmpty(), norm)
     assert out.num_rbf() > 0
     assert float(final) < float(empty_loss)
+
+
+class _CheckedRender:
+    """MeshRenderConfocal (the GPU path, whose results the loop uses) with each
+    forward it computes compared on the spot with the FP64 oracle at the same
+    inputs, and each gradient recorded beside the oracle's gradient for the
+    same upstream cotangent (compared after the loop)."""
+
+    def __init__(self):
+        self.forward_errors, self.entries = [], []
+
+    def apply(self, verts, faces, scan_points, bin_def, colors=None, scan_origin=None):
+        if verts.requires_grad:  # not for the loop's untracked intensity render
+            verts.retain_grad()
+            colors.retain_grad()
+        y = MeshRenderConfocal.apply(verts, faces, scan_points, bin_def, colors, scan_origin)
+        v = verts[0].detach().cpu().numpy()
+        f = faces[0].cpu().numpy()
+        sp = scan_points[0].cpu().numpy()
+        c = colors[0].detach().cpu().numpy()
+        bd = bin_def
+        vis = oracle.mesh_visibility(v, f, sp)
+        ref = oracle.mesh_confocal_forward(v, f, c, sp, None, vis, bd.num, bd.width, bd.offset)
+        self.forward_errors.append(rel_l2(y[0].detach().cpu().numpy(), ref))
+        entry = {"verts": verts, "colors": colors}
+
+        def hook(g):
+            entry["ref"] = oracle.mesh_confocal_grad(v, f, c, sp, None, vis, bd.num, bd.width,
+                                                     bd.offset, g[0].cpu().numpy())
+        if y.requires_grad:
+            y.register_hook(hook)
+        self.entries.append(entry)
+        return y
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_depth_map_loop_matches_the_oracle_at_every_step(cuda_lib, monkeypatch):
+    """Eight steps of the depth-map fit: at every parameter state the loop
+    visits, the GPU render equals the FP64 oracle's (1e-5) and so do the
+    vertex and albedo gradients for that step's cotangent (1e-5). Two
+    independently driven runs are not compared: Adam's first steps have the
+    size of the learning rate for any gradient sign, so rounding-level
+    gradient differences on near-zero entries would show as whole steps."""
+    from totri_gb300.fitting import DepthMap, DepthMapFitting
+    from totri_gb300.fitting import depth_map as dm_module
+    from totri_gb300.types import VolumeDef
+    vd, truth, _, _, bd, target = _bump_target(res=10)
+    sp = scenes.wall_grid(12)[0].cuda()
+    with torch.no_grad():
+        target = MeshRenderConfocal.apply(truth.verts()[None], truth.faces[None], sp[None], bd,
+                                          truth.color.view(1, -1, 1))[0]
+    checked = _CheckedRender()
+    monkeypatch.setattr(dm_module, "MeshRenderConfocal", checked)
+    dm = DepthMap(VolumeDef(vd.start, vd.end, vd.resolution))
+    fit = DepthMapFitting(bd)
+    fit.fit(dm, target, sp, num_iter=8, lambda_depth=0.02, lambda_color=0.01)
+    # one untracked render for the intensity, then one per step
+    assert len(checked.forward_errors) == 9
+    assert max(checked.forward_errors) < 1e-5, checked.forward_errors
+    graded = [e for e in checked.entries if "ref" in e]
+    assert len(graded) == 8
+    for e in graded:
+        rv, rm = e["ref"]
+        assert rel_l2(e["verts"].grad[0].cpu().numpy(), rv) < 1e-5
+        assert rel_l2(e["colors"].grad[0].cpu().numpy(), rm) < 1e-5
+    assert float(fit.losses[-1]) < float(fit.losses[0])
+
+
+def _robust_same(a, b, lr_bound):
+    """Two runs of an Adam loop whose gradients differ by summation order
+    (30 steps of a 12 x 12 depth map differ by a median 6.5e-5): half the
+    entries within a tenth of one learning-rate step, the rest by at most the
+    steps taken."""
+    d = (a - b).abs().flatten()
+    assert float(d.median()) <= 1e-3
+    assert float(d.max()) <= lr_bound
+
+
+def test_fit_depth_map_request_alone_and_in_the_mix(cuda_lib):
+    from totri_gb300.fitting import DepthMap, DepthMapFitting
+    from totri_gb300.serve import Request, Server
+    from totri_gb300.types import VolumeDef
+    vd, truth, sp, _, bd, target = _bump_target(res=12)
+    other = scenes.displaced_sphere(3, 9)
+    srv = Server(hbm_budget=8e9, slots=3)
+    srv.register_mesh("o", other[0][0], other[1][0])
+    srv.register_grid("g", sp.cpu())
+    srv.register_measurement("t", target.cpu(), "g", bd)
+    req = lambda: Request("fit_depth_map", "g", bins=bd, target="t", volume=vd,  # noqa: E731
+                          iterations=30)
+    with srv:
+        alone = srv.submit(req()).result()
+        futs = [srv.submit(Request("render", "g", mesh="o", bins=bd)) for _ in range(3)]
+        mixed = srv.submit(req())
+        futs += [srv.submit(Request("grad", "g", mesh="o", bins=bd, target="t"))
+                 for _ in range(3)]
+        mixed = mixed.result()
+        for fu in futs:
+            fu.result()
+    dm = DepthMap(VolumeDef(vd.start, vd.end, vd.resolution))
+    direct = DepthMapFitting(bd)
+    direct.fit(dm, target, sp, num_iter=30)
+    losses = torch.stack(direct.losses).cpu()
+    for run in (alone, mixed):
+        assert run[0].shape == (12, 12) and run[2].shape == (30,)
+        _robust_same(run[0], dm.depth.cpu(), 2 * 1e-2 * 30)
+        _robust_same(run[1], dm.color.cpu(), 2 * 1e-2 * 30)
+        assert float((run[2] - losses).abs().max()) <= 1e-3 * float(losses.max())
+    assert float(alone[2][-1]) < float(alone[2][0])
+
+
+def test_fit_rbf_request_runs_beside_other_requests(cuda_lib):
+    """A blob fit served on its worker thread: it adds blobs and lowers the
+    loss below the empty set's, and the renders submitted beside it equal the
+    same renders served alone."""
+    from totri_gb300.fitting import GaussianRbfBase, RbfFitting, TransientBackgroundEmpty
+    from totri_gb300.serve import Request, Server
+    from totri_gb300.types import VolumeDef
+    vd, truth, sp, bd = _rbf_problem()
+    fit = RbfFitting(bd, sp)
+    with torch.no_grad():
+        target = fit.base_to_transient(truth, TransientBackgroundEmpty(),
+                                       torch.ones(1, device="cuda"))[1]
+    norm = target / target.mean()
+    empty_loss = float(fit.loss_all(GaussianRbfBase(VolumeDef(vd.start, vd.end, vd.resolution)),
+                                    TransientBackgroundEmpty(), norm)[0]["data"])
+    other = scenes.displaced_sphere(3, 9)
+    srv = Server(hbm_budget=8e9, slots=2, large_slots=1)
+    srv.register_mesh("o", other[0][0], other[1][0])
+    srv.register_grid("g", sp.cpu())
+    srv.register_measurement("t", target.cpu(), "g", bd)
+    with srv:
+        ref = srv.submit(Request("render", "g", mesh="o", bins=bd)).result()
+        blob = srv.submit(Request("fit_rbf", "g", bins=bd, target="t", volume=vd, iterations=2,
+                                  seed=5))
+        renders = [srv.submit(Request("render", "g", mesh="o", bins=bd)) for _ in range(4)]
+        params, loss = blob.result()
+        renders = [fu.result() for fu in renders]
+    assert any(r.kind == "fit_rbf" and r.large for r in srv.completed)
+    assert params.shape[0] > 0 and params.shape[1] == 4
+    assert float(loss) < empty_loss
+    for r in renders:
+        assert torch.allclose(r, ref, rtol=1e-5, atol=1e-6 * float(ref.abs().max()))

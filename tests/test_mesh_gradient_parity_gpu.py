@@ -215,13 +215,22 @@ def exhaustive_large(cuda_lib):
     return dict(n=n, d=d, bd=bd, ref=ref, tg=torch.from_numpy(tg)[None].cuda(), rv=rv, rm=rm)
 
 
+_SPLAT_VARIANTS = [{}, {"mesh.exhaustive.splat.occupancy": 1}]
+
+
+@pytest.mark.parametrize("keys", _SPLAT_VARIANTS, ids=lambda k: ",".join(
+    "%s=%d" % (a.split(".")[-1], b) for a, b in k.items()) or "default")
 @pytest.mark.parametrize("lt", autotune.CANDIDATES["mesh.exhaustive.splat.lt"])
-def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt):
+def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt, keys):
+    """Every laser tile, with the register-capped splat (the default) or the
+    uncapped one ("mesh.exhaustive.splat.occupancy" = 1)."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]
     empty = torch.empty_like(d["sp"][:, :0])
     out = torch.full((1, bd.num, d["sp"].shape[1], d["lp"].shape[1]), 3.0, device="cuda")
     autotune.set_tile("mesh.exhaustive.splat.lt", lt)
+    for k, v in keys.items():
+        autotune.set_tile(k, v)
     try:
         call = lambda: R.mesh_exhaustive_forward(  # noqa: E731
             d["verts"], d["faces"], d["colors"], d["sp"], d["lp"], empty, empty, out, bd.width,
@@ -235,24 +244,36 @@ def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt):
         call()
     finally:
         autotune.set_tile("mesh.exhaustive.splat.lt", 0)
+        for k in keys:
+            autotune.set_tile(k, 0)
     assert rel_l2(out[0].double().cpu().numpy(), w["ref"]) < FWD_TOL
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
-def test_exhaustive_large_gradient_matches_fp64_oracle(exhaustive_large, mode):
+_GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.mode": 2},
+                  {"mesh.exhaustive.grad.occupancy": 4}, {"mesh.exhaustive.grad.faces": 1},
+                  {"mesh.exhaustive.grad.faces": 5}, {"mesh.exhaustive.grad.faces": 32}]
+
+
+@pytest.mark.parametrize("keys", _GRAD_VARIANTS, ids=lambda k: ",".join(
+    "%s=%d" % (a.split(".")[-1], b) for a, b in k.items()) or "default")
+def test_exhaustive_large_gradient_matches_fp64_oracle(exhaustive_large, keys):
     """The three gradient kernels (separable point records, the default;
-    per-lane mask tests; compacted triples) against the FP64 oracle."""
+    per-lane mask tests; compacted triples) and the point-record kernel's
+    register cap and faces-per-CTA shapes (including counts that do not
+    divide the face count) against the FP64 oracle."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]
     empty = torch.empty_like(d["sp"][:, :0])
     vg = torch.full_like(d["verts"], 2.0)
     mg = torch.full_like(d["colors"], 2.0)
-    autotune.set_tile("mesh.exhaustive.grad.mode", mode)
+    for k, v in keys.items():
+        autotune.set_tile(k, v)
     try:
         R.mesh_exhaustive_grad_verts(d["verts"], d["faces"], d["colors"], d["sp"], d["lp"], empty,
                                      empty, w["tg"], vg, mg, bd.width, bd.offset, 0)
     finally:
-        autotune.set_tile("mesh.exhaustive.grad.mode", 0)
+        for k in keys:
+            autotune.set_tile(k, 0)
     ev = rel_l2(vg[0].double().cpu().numpy(), w["rv"])
     em = rel_l2(mg[0].double().cpu().numpy(), w["rm"])
     print("exhaustive gradient rel-L2: vertices %.3e, albedo %.3e" % (ev, em))

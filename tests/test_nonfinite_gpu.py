@@ -183,3 +183,22 @@ def test_device_still_answers(cuda_lib):
     ref = oracle.mesh_confocal_forward(n["verts"], n["faces"], n["colors"], n["scan_points"],
                                        None, vis, bd.num, bd.width, bd.offset)
     assert rel_l2(out[0].cpu().numpy(), ref) < 1e-5
+
+
+def test_volume_with_degenerate_bin_width(cuda_lib):
+    """A zero or NaN bin width: every bin is walked (zero: all bins share one
+    centre, the offset), matching the oracle; no hang, no fault."""
+    g = np.random.default_rng(10)
+    X, N, T = 8, 20, 40
+    vol = ((g.random((X, X, X)) < 0.2) * g.random((X, X, X))).astype(np.float32)
+    mp = np.stack([g.uniform(-1, 1, N), g.uniform(-1, 1, N), np.zeros(N)]).astype(np.float32)
+    org, size = (-0.5, -0.5, 0.5), (1.0, 1.0, 1.0)
+    y = g.standard_normal((N, T)).astype(np.float32)
+    for bw, bo in ((0.0, 1.1), (float("nan"), 0.0), (float("inf"), 0.0), (0.03, float("nan"))):
+        out = torch.full((N, T), 3.0, device="cuda")
+        R.volume_confocal_forward(cu(vol), cu(mp), out, org, size, bw, bo)
+        same(out.cpu().numpy(), oracle.volume_confocal_forward(vol, mp, T, org, size, bw, bo))
+        adj = torch.full(vol.shape, 3.0, device="cuda")
+        R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+        same(adj.cpu().numpy(),
+             oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo))

@@ -181,3 +181,120 @@ def test_filtered_samples_keep_exact_cells(cuda_lib):
     for a, b in ((ta, tb), (aa, ab)):
         assert rel(a.numpy(), b.numpy()) < 1e-5
         assert float((a - b).abs().max()) <= 2e-4 * float(b.abs().max())
+
+
+def column_case(Z, seed, bo=0.0, N=36, lift=False):
+    """A 6 x 5 x Z volume over [-0.5, 0.5]^2 x [0.5, 1.5] m, N points on
+    [-1, 1]^2 (heights 0, or up to 1.2 m with lift, so that some columns
+    start below a point), 0.01 m bins to 3 m past the offset."""
+    g = np.random.default_rng(seed)
+    vol = ((g.random((6, 5, Z)) < 0.3) * g.random((6, 5, Z))).astype(np.float32)
+    wz = g.uniform(0.0, 1.2, N) if lift else np.zeros(N)
+    mp = np.stack([g.uniform(-1, 1, N), g.uniform(-1, 1, N), wz]).astype(np.float32)
+    T = int(round((3.0 - bo) / 0.01))
+    return vol, mp, (-0.5, -0.5, 0.5), (1.0, 1.0, 1.0), T, 0.01, bo
+
+
+@pytest.mark.parametrize("Z", [1, 19, 32, 40, 100, 128, 200, 256, 300])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_adjoint_kernels_match_oracle(cuda_lib, Z, mode):
+    """The three adjoint kernels ("volume.adjoint.mode": 0 lanes over 32
+    columns, the default; 1 shared-memory atomics; 2 lane-owned cells, for
+    columns of up to 256 cells, else the atomic kernel) against the FP64 exact
+    adjoint, at column depths that take every cells-per-lane variant and its
+    edges, on a 6 x 5 column grid (a partial 8 x 4 tile), with points below
+    and inside the volume's height range."""
+    from totri_gb300 import autotune
+    vol, mp, org, size, T, bw, bo = column_case(Z, seed=Z, lift=True)
+    y = np.random.default_rng(Z + 1).standard_normal((mp.shape[1], T)).astype(np.float32)
+    ref = oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo)
+    autotune.set_tile("volume.adjoint.mode", mode)
+    try:
+        adj = torch.full(vol.shape, 7.0, device="cuda")
+        R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+    finally:
+        autotune.set_tile("volume.adjoint.mode", 0)
+    got = adj.cpu().numpy()
+    if Z == 1:  # a single cell has no interpolation pair: no samples
+        assert not got.any() and not ref.any()
+        return
+    # the interpolation weight z_hat - floor(z_hat) keeps the FP32 rounding of
+    # z_hat in [0, Z) (the reference's arithmetic), an absolute error that
+    # grows with the column depth: 1e-5 up to 200 cells, in proportion beyond
+    assert rel(got, ref) < 1e-5 * max(1.0, Z / 200.0)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_negative_bin_offset(cuda_lib, mode):
+    """With a negative bin offset the first bins have negative centres; their
+    samples (the centre squared, as the reference computes them) reach the
+    volume when |offset| exceeds a point's horizontal distance to a column.
+    Forward, adjoint (both kernels) and measurement-point gradient against the
+    FP64 oracle, which walks every bin."""
+    from totri_gb300 import autotune
+    vol, mp, org, size, T, bw, bo = column_case(48, seed=5, bo=-1.0)
+    out = torch.full((mp.shape[1], T), 3.0, device="cuda")
+    R.volume_confocal_forward(cu(vol), cu(mp), out, org, size, bw, bo)
+    ref = oracle.volume_confocal_forward(vol, mp, T, org, size, bw, bo)
+    assert np.abs(ref[:, :100]).sum() > 0.05 * np.abs(ref).sum()  # negative centres count
+    assert rel(out.cpu().numpy(), ref) < 1e-5
+    y = np.random.default_rng(6).standard_normal((mp.shape[1], T)).astype(np.float32)
+    autotune.set_tile("volume.adjoint.mode", mode)
+    try:
+        adj = torch.empty(vol.shape, device="cuda")
+        R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+    finally:
+        autotune.set_tile("volume.adjoint.mode", 0)
+    assert rel(adj.cpu().numpy(),
+               oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo)) < 1e-5
+    gm = torch.empty((3, mp.shape[1]), device="cuda")
+    R.volume_confocal_grad_measurement_points(gm, cu(vol), cu(mp), cu(y), org, size, bw, bo)
+    assert rel(gm.cpu().numpy(), oracle.volume_confocal_grad_mp(vol, mp, y, org, size, bw,
+                                                                bo)) < 1e-4
+
+
+def test_adjoint_kernels_full_size_agree(cuda_lib):
+    """128^3 voxels x 128x128 points x 1024 bins: the three adjoint kernels
+    agree to FP32 summation order (the same samples, each decided by the
+    exact chain)."""
+    from totri_gb300 import autotune
+    s = scenes.volume_scene()
+    vd, bd = s["volume_def"], s["bin_def"]
+    size = tuple(e - a for a, e in zip(vd.start, vd.end))
+    mp = s["scan_points"][0].T.contiguous().cuda()
+    y = torch.randn((mp.shape[1], bd.num), device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(21))
+    out = []
+    for mode in (0, 1, 2):
+        autotune.set_tile("volume.adjoint.mode", mode)
+        try:
+            adj = torch.empty((128, 128, 128), device="cuda")
+            R.volume_confocal_adjoint(adj, mp, y, vd.start, size, bd.width, bd.offset)
+            out.append(adj.cpu().numpy())
+        finally:
+            autotune.set_tile("volume.adjoint.mode", 0)
+    assert rel(out[0], out[1]) < 1e-5
+    assert rel(out[2], out[1]) < 1e-5
+
+
+@pytest.mark.parametrize("warps", [1, 3, 8])
+def test_adjoint_columns_kernel_block_shapes(cuda_lib, warps):
+    """The lanes-over-columns adjoint with 1, 3 and 8 warps per CTA (its
+    point groups and per-warp column copies) against the FP64 exact adjoint,
+    on a 13 x 9 column grid (partial tiles in both directions)."""
+    from totri_gb300 import autotune
+    g = np.random.default_rng(warps)
+    vol = np.zeros((13, 9, 70), np.float32)
+    N = 150
+    mp = np.stack([g.uniform(-1, 1, N), g.uniform(-1, 1, N), g.uniform(0, 0.8, N)]).astype(
+        np.float32)
+    org, size, T, bw, bo = (-0.5, -0.5, 0.5), (1.0, 1.0, 1.0), 300, 0.01, 0.0
+    y = g.standard_normal((N, T)).astype(np.float32)
+    ref = oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo)
+    autotune.set_tile("volume.adjoint.warps", warps)
+    try:
+        adj = torch.full(vol.shape, 5.0, device="cuda")
+        R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+    finally:
+        autotune.set_tile("volume.adjoint.warps", 0)
+    assert rel(adj.cpu().numpy(), ref) < 1e-5

@@ -548,9 +548,10 @@ __device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* tota
   return flag ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
 }
 
-__global__ void __launch_bounds__(256, 3) exh_grad_face_kernel(
+template <int kOcc>
+__global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
     Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
-    int T, float bw, float bo, GradOut out) {
+    int T, float bw, float bo, GradOut out, int faces_per_cta) {
   extern __shared__ float recs[];        // scan-point then laser-point records, SoA
   float* srec = recs;
   float* lrec = recs + kRec * kFaceSlice;
@@ -567,8 +568,8 @@ __global__ void __launch_bounds__(256, 3) exh_grad_face_kernel(
   const float4* shade = sc.shade + (size_t)b * sc.F * 4;
   const uint32_t* mrows = sc.mask + (size_t)b * sc.P * sc.nch;
   const float inv_bw = __frcp_rn(bw);
-  for (int fi = 0; fi < kFacesPerCta; ++fi) {
-    const int k = blockIdx.x * kFacesPerCta + fi;
+  for (int fi = 0; fi < faces_per_cta; ++fi) {
+    const int k = blockIdx.x * faces_per_cta + fi;
     if (k >= n) break;  // CTA-uniform
     const float4 s0r = __ldg(shade + 4 * k), s1r = __ldg(shade + 4 * k + 1);
     const float4 s2r = __ldg(shade + 4 * k + 2), s3r = __ldg(shade + 4 * k + 3);
@@ -831,14 +832,27 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   // 32-mesh batch).
   const int mode = tune::get("mesh.exhaustive.grad.mode");
   if (mode != 1 && mode != 2) {
+    // "mesh.exhaustive.grad.faces": faces per CTA (default 8);
+    // "mesh.exhaustive.grad.occupancy" = 4: registers capped for 4 CTAs per SM
+    // (64, with spills) instead of 3 (80)
+    const int fpc = tune::get("mesh.exhaustive.grad.faces") > 0
+                        ? (int)tune::get("mesh.exhaustive.grad.faces")
+                        : kFacesPerCta;
+    const bool occ4 = tune::get("mesh.exhaustive.grad.occupancy") == 4;
+    const void* fn = occ4 ? reinterpret_cast<const void*>(exh_grad_face_kernel<4>)
+                          : reinterpret_cast<const void*>(exh_grad_face_kernel<3>);
     const size_t smem = sizeof(float) * 2 * kRec * kFaceSlice;
-    TOTRI_CUDA(tune::ensure_dynamic_smem(reinterpret_cast<const void*>(exh_grad_face_kernel),
-                                         smem));
-    const dim3 grid((unsigned)ceil_div(sc.F, kFacesPerCta), (unsigned)sc.B,
+    TOTRI_CUDA(tune::ensure_dynamic_smem(fn, smem));
+    const dim3 grid((unsigned)ceil_div(sc.F, fpc), (unsigned)sc.B,
                     (unsigned)ceil_div(S, kFaceSlice));
-    TOTRI_KERNEL("mesh exhaustive grad", stream,
-                 exh_grad_face_kernel<<<grid, 256, smem, stream>>>(sc, sp, lp, org, S, L, tgrad, T,
-                                                                   bw, bo, out));
+    if (occ4)
+      TOTRI_KERNEL("mesh exhaustive grad", stream,
+                   exh_grad_face_kernel<4><<<grid, 256, smem, stream>>>(
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc));
+    else
+      TOTRI_KERNEL("mesh exhaustive grad", stream,
+                   exh_grad_face_kernel<3><<<grid, 256, smem, stream>>>(
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc));
     return TOTRI_OK;
   }
   if (mode == 1) {

@@ -1,13 +1,33 @@
-// Tile-shape overrides (see tune.cu). Keys:
+// Tile-shape and kernel-variant overrides (see tune.cu); 0 (unset) takes the
+// default. Keys:
 //   "mesh.confocal.splat.ts"    scan points per confocal splat CTA (1,2,4,8,16)
+//   "mesh.confocal.splat.mode"  confocal splat variant (at its launcher)
+//   "mesh.confocal.exact"       1: every confocal sample takes the exact chain
+//   "mesh.confocal.grad.split"  scan-point slices per confocal gradient chunk
 //   "mesh.exhaustive.splat.lt"  laser points per exhaustive splat CTA (1,4,8,16,32)
-//   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
+//   "mesh.exhaustive.splat.mode", "mesh.exhaustive.splat.occupancy"
+//                               exhaustive splat variant / 1: uncapped registers
+//   "mesh.exhaustive.exact"     1: every exhaustive sample takes the exact chain
+//   "mesh.exhaustive.grad.mode" 1 per-lane mask tests, 2 compacted triples
+//                               (default: per-face point records)
+//   "mesh.exhaustive.grad.faces" faces per CTA of the point-record gradient (8)
+//   "mesh.exhaustive.grad.occupancy" 4: that kernel capped for 4 CTAs/SM (64
+//                               registers) instead of 3
+//   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
 //   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk
 //   "mesh.visibility.queue"     1: queued BVH searches (visibility_queue_kernel)
 //   "mesh.visibility.wide"      2: binary BVH search after the surface-walk prefix
 //                               (the default is the 4-wide search)
-//   "mesh.confocal.grad.split"  scan-point slices per confocal gradient chunk
-//   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
+//   "mesh.visibility.occupancy", ".chunks", ".seed", ".seed.steps", ".shaft.cap"
+//                               visibility launch shape and prefix (at its launcher)
+//   "volume.exact"              1: every volume sample takes the exact chain
+//   "volume.adjoint.mode"       0 lanes over 32 columns (default), 1 shared-memory
+//                               atomics, 2 lane-owned cells (up to 256 cells)
+//   "volume.adjoint.warps"      warps per CTA of the lanes-over-columns adjoint
+//   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
+//   "backprojection.velten.mode", ".occupancy", ".vz"
+//                               Velten kernel variant, 1: uncapped registers, slab depth
+//   "rbf.cull"                  1: RBF kernels without the underflow cull
 #pragma once
 
 #include <cuda_runtime.h>

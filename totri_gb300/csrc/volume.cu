@@ -9,6 +9,9 @@
 // (voxel, point), found by inverting the sphere/column geometry and then
 // re-deciding each bin with the reference's FP32 sample arithmetic. Each CTA
 // owns a tile of points and keeps their transient rows in shared memory.
+#include <algorithm>
+#include <climits>
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -23,8 +26,10 @@ struct Geo {
   float ox, oy, oz, sx, sy, sz;
   float scale;  // Z / sz
   float bw, bo;
+  float inv_bw;
   int T;
-  int exact;  // 1: every sample takes the exact chain (tuning key "volume.exact")
+  int exact;     // 1: every sample takes the exact chain (tuning key "volume.exact")
+  int all_bins;  // bin width not positive and finite (or offset not finite): walk every bin
 };
 
 // Column / slice centre: origin + ((i + 0.5) * size) / n (volume_cuda.cu:35,38).
@@ -98,22 +103,64 @@ __device__ __forceinline__ Sample sample_filtered(const Geo& g, float wx, float 
   return s;
 }
 
+// First bin whose centre t bw + bo (the sample chain's FP32 arithmetic) is not
+// negative; 0 unless the bin offset is negative. Bins before it have negative
+// centres, whose samples mirror those of the positive centres (the reference
+// walks every bin and squares the centre).
+__device__ __forceinline__ int first_nonneg_bin(const Geo& g) {
+  if (g.all_bins || !(g.bo < 0.f)) return 0;
+  const float tf = ceilf(-g.bo * g.inv_bw);
+  if (!(tf < (float)g.T)) return g.T;
+  int t = max((int)tf - 2, 0);
+  while (t > 0 && xadd(xmul((float)(t - 1), g.bw), g.bo) >= 0.f) --t;
+  while (t < g.T && xadd(xmul((float)t, g.bw), g.bo) < 0.f) ++t;
+  return t;
+}
+
+// Bins whose centre's magnitude lies in [cl, ch] widened by eps bins: [p0, p1]
+// with non-negative centres (t >= tz) and [n0, n1] with negative ones (t < tz).
+// Every bin when the bin width is degenerate. A NaN bound gives empty spans.
+struct Spans {
+  int p0, p1, n0, n1;
+};
+__device__ __forceinline__ Spans tc_spans(const Geo& g, int tz, float cl, float ch, float eps) {
+  Spans s{1, 0, 1, 0};
+  if (g.all_bins) {
+    s.p0 = 0;
+    s.p1 = g.T - 1;
+    return s;
+  }
+  if (!(cl <= ch)) return s;
+  s.p0 = max(__float2int_ru((cl - g.bo) * g.inv_bw - eps), tz);
+  s.p1 = min(__float2int_rd((ch - g.bo) * g.inv_bw + eps), g.T - 1);
+  if (tz > 0) {
+    s.n0 = max(__float2int_ru((-ch - g.bo) * g.inv_bw - eps), 0);
+    s.n1 = min(__float2int_rd((-cl - g.bo) * g.inv_bw + eps), tz - 1);
+  }
+  return s;
+}
+
+// Centre magnitudes [cl, ch] of the bins whose samples from a point at squared
+// horizontal distance rho2 and height wz can land in z in [zlo, zhi); false
+// when the whole interval lies below the point.
+__device__ __forceinline__ bool tc_bounds(float rho2, float wz, float zlo, float zhi, float& cl,
+                                          float& ch) {
+  const float dhi = zhi - wz;
+  if (!(dhi > 0.f)) return false;
+  const float dlo = fmaxf(zlo - wz, 0.f);
+  cl = sqrtf(dlo * dlo + rho2);
+  ch = sqrtf(dhi * dhi + rho2);
+  return true;
+}
+
 // Bins whose sample may fall in interpolation cells k-1 or k of a column
 // (conservative: one extra bin each side).
-__device__ __forceinline__ void bin_range(const Geo& g, float rho2, float wz, int k, int& t0,
-                                          int& t1) {
-  const float zlo = g.oz + ((float)k - 0.5f) / g.scale;
-  const float zhi = g.oz + ((float)k + 1.5f) / g.scale;
-  const float dhi = zhi - wz;
-  if (!(dhi > 0.f)) {
-    t0 = 1;
-    t1 = 0;
-    return;
-  }
-  const float dlo = fmaxf(zlo - wz, 0.f);
-  const float tclo = sqrtf(dlo * dlo + rho2), tchi = sqrtf(dhi * dhi + rho2);
-  t0 = max((int)floorf((tclo - g.bo) / g.bw) - 1, 0);
-  t1 = min((int)ceilf((tchi - g.bo) / g.bw) + 1, g.T - 1);
+__device__ __forceinline__ Spans bin_range(const Geo& g, int tz, float rho2, float wz, int k) {
+  float cl, ch;
+  if (!tc_bounds(rho2, wz, g.oz + ((float)k - 0.5f) / g.scale,
+                 g.oz + ((float)k + 1.5f) / g.scale, cl, ch))
+    return Spans{1, 0, 1, 0};
+  return tc_spans(g, tz, cl, ch, 1.f);
 }
 
 struct Points {  // measurement points [3, N] with strides
@@ -149,6 +196,7 @@ __global__ void __launch_bounds__(256) confocal_forward_kernel(
   const uint32_t nnz = *count;
   const int pl = threadIdx.x % kPT;
   const int i = i0 + pl;
+  const int tz = first_nonneg_bin(g);
   if (i < N) {
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
     float* row = hist + pl * g.T;
@@ -159,16 +207,18 @@ __global__ void __launch_bounds__(256) confocal_forward_kernel(
       const float val = __ldg(vol + lin);
       const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
       const float rho2 = (wx - x) * (wx - x) + (wy - y) * (wy - y);
-      int t0, t1;
-      bin_range(g, rho2, wz, k, t0, t1);
-      for (int t = t0; t <= t1; ++t) {
-        const Sample s = sample(g, wx, wy, wz, t, x, y);
-        if (!s.ok) continue;
-        float w;
-        if (s.zi == k) w = 1.f - s.alpha;
-        else if (s.zi == k - 1) w = s.alpha;
-        else continue;
-        atomicAdd(row + t, val * w * s.f2);
+      const Spans sp = bin_range(g, tz, rho2, wz, k);
+      for (int r = 0; r < 2; ++r) {
+        const int t0 = r ? sp.n0 : sp.p0, t1 = r ? sp.n1 : sp.p1;
+        for (int t = t0; t <= t1; ++t) {
+          const Sample s = sample(g, wx, wy, wz, t, x, y);
+          if (!s.ok) continue;
+          float w;
+          if (s.zi == k) w = 1.f - s.alpha;
+          else if (s.zi == k - 1) w = s.alpha;
+          else continue;
+          atomicAdd(row + t, val * w * s.f2);
+        }
       }
     }
   }
@@ -195,6 +245,7 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
   const int pl = threadIdx.x % kPT;
   const int i = i0 + pl;
   float gx = 0.f, gy = 0.f, gz = 0.f;
+  const int tz = first_nonneg_bin(g);
   if (i < N) {
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
     const float* trow = tg + (size_t)i * g.T;
@@ -205,24 +256,27 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
       const float val = __ldg(vol + lin);
       const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
       const float rho2 = (wx - x) * (wx - x) + (wy - y) * (wy - y);
-      int t0, t1;
-      bin_range(g, rho2, wz, k, t0, t1);
-      for (int t = t0; t <= t1; ++t) {
-        const Sample s = sample(g, wx, wy, wz, t, x, y);
-        if (!s.ok || (s.zi != k && s.zi != k - 1)) continue;
-        const float tc = (float)t * g.bw + g.bo;
-        const float depth = sqrtf(fmaxf(tc * tc - (wx - x) * (wx - x) - (wy - y) * (wy - y), 0.f));
-        const float dzx = -(wx - x) / depth, dzy = -(wy - y) / depth;
-        const float tc2 = tc * tc, tc4 = tc2 * tc2;
-        const float df2 = 4.f * depth * depth * depth / (tc4 * tc4);
-        // this voxel is the lower (zi == k) or upper (zi == k-1) interpolation node
-        const bool lower = s.zi == k;
-        const float wgt = lower ? 1.f - s.alpha : s.alpha;
-        const float sgn = lower ? -1.f : 1.f;
-        const float dl = __ldg(trow + t) * val;
-        gx += dl * (wgt * df2 * dzx + sgn * g.scale * dzx * s.f2);
-        gy += dl * (wgt * df2 * dzy + sgn * g.scale * dzy * s.f2);
-        gz += dl * (sgn * g.scale * s.f2);
+      const Spans sp = bin_range(g, tz, rho2, wz, k);
+      for (int r = 0; r < 2; ++r) {
+        const int t0 = r ? sp.n0 : sp.p0, t1 = r ? sp.n1 : sp.p1;
+        for (int t = t0; t <= t1; ++t) {
+          const Sample s = sample(g, wx, wy, wz, t, x, y);
+          if (!s.ok || (s.zi != k && s.zi != k - 1)) continue;
+          const float tc = (float)t * g.bw + g.bo;
+          const float depth =
+              sqrtf(fmaxf(tc * tc - (wx - x) * (wx - x) - (wy - y) * (wy - y), 0.f));
+          const float dzx = -(wx - x) / depth, dzy = -(wy - y) / depth;
+          const float tc2 = tc * tc, tc4 = tc2 * tc2;
+          const float df2 = 4.f * depth * depth * depth / (tc4 * tc4);
+          // this voxel is the lower (zi == k) or upper (zi == k-1) interpolation node
+          const bool lower = s.zi == k;
+          const float wgt = lower ? 1.f - s.alpha : s.alpha;
+          const float sgn = lower ? -1.f : 1.f;
+          const float dl = __ldg(trow + t) * val;
+          gx += dl * (wgt * df2 * dzx + sgn * g.scale * dzx * s.f2);
+          gy += dl * (wgt * df2 * dzy + sgn * g.scale * dzy * s.f2);
+          gz += dl * (sgn * g.scale * s.f2);
+        }
       }
     }
   }
@@ -247,22 +301,22 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
 // Bins whose samples can land in any interpolation cell of a column seen from
 // a point at squared horizontal distance rho2 and height wz: cells 0 .. Z-2
 // hold z in [oz + 0.5/scale, oz + (Z - 0.5)/scale), widened by one cell above
-// and one bin each side (bin_range's span for cells 1 and Z - 1). Empty
-// (t0 > t1) when the whole column lies below the point.
-__device__ __forceinline__ void column_span(const Geo& g, float rho2, float wz, int& t0,
-                                            int& t1) {
-  const float zlo = g.oz + 0.5f / g.scale;
-  const float zhi = g.oz + ((float)g.Z + 0.5f) / g.scale;
-  const float dhi = zhi - wz;
-  if (!(dhi > 0.f)) {
-    t0 = 1;
-    t1 = 0;
-    return;
-  }
-  const float dlo = fmaxf(zlo - wz, 0.f);
-  const float tclo = sqrtf(dlo * dlo + rho2), tchi = sqrtf(dhi * dhi + rho2);
-  t0 = max((int)floorf((tclo - g.bo) / g.bw) - 1, 0);
-  t1 = min((int)ceilf((tchi - g.bo) / g.bw) + 1, g.T - 1);
+// and one bin each side (bin_range's spans for cells 1 and Z - 1).
+__device__ __forceinline__ Spans column_span(const Geo& g, int tz, float rho2, float wz) {
+  float cl, ch;
+  if (!tc_bounds(rho2, wz, g.oz + 0.5f / g.scale, g.oz + ((float)g.Z + 0.5f) / g.scale, cl, ch))
+    return Spans{1, 0, 1, 0};
+  return tc_spans(g, tz, cl, ch, 1.f);
+}
+
+// Largest |t bw + bo| over the bins of two spans (0 when both are empty).
+__device__ __forceinline__ float span_tc_max(const Geo& g, const Spans& s) {
+  float m = 0.f;
+  if (s.p0 <= s.p1)
+    m = fmaxf(fabsf((float)s.p1 * g.bw + g.bo), fabsf((float)s.p0 * g.bw + g.bo));
+  if (s.n0 <= s.n1)
+    m = fmaxf(m, fmaxf(fabsf((float)s.n1 * g.bw + g.bo), fabsf((float)s.n0 * g.bw + g.bo)));
+  return m;
 }
 
 // Exact adjoint of the forward: one CTA per voxel column, a warp per point at a
@@ -289,11 +343,12 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
   float* col = cols + warp * g.Z;
   const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
   const float u = 5.9604645e-8f;
+  const int tz = first_nonneg_bin(g);
   for (int base = warp * 32; base < N; base += 256) {
     // lane j prepares point base + j
     const int ip = base + lane;
     float wx = 0.f, wy = 0.f, wz = 0.f, ddx = 0.f, ddy = 0.f, marg = 0.f;
-    int ta = 1, tb = 0;
+    Spans sp{1, 0, 1, 0};
     if (ip < N) {
       wx = mp.at(0, ip);
       wy = mp.at(1, ip);
@@ -301,11 +356,10 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
       const float dx = xsub(wx, x), dy = xsub(wy, y);
       ddx = xmul(dx, dx);
       ddy = xmul(dy, dy);
-      column_span(g, dx * dx + dy * dy, wz, ta, tb);
+      sp = column_span(g, tz, dx * dx + dy * dy, wz);
       // sample_filtered's margin 8 u scale (depth + |wz| + |z| + |oz|) + 4 u |zh|
-      // + 1e-7 with depth, |z| and |zh| at their largest over the span's bins
-      const float tcm = fmaxf(fabsf((float)tb * g.bw + g.bo), fabsf((float)ta * g.bw + g.bo));
-      const float dmax = 1.001f * tcm;
+      // + 1e-7 with depth, |z| and |zh| at their largest over the spans' bins
+      const float dmax = 1.001f * span_tc_max(g, sp);
       const float zmax = fabsf(wz) + dmax;
       const float zhmax = (zmax + fabsf(g.oz)) * g.scale + 0.5f;
       marg = 8.f * u * g.scale * (dmax + fabsf(wz) + zmax + fabsf(g.oz)) + 4.f * u * zhmax +
@@ -313,37 +367,41 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
     }
     const int np = min(32, N - base);
     for (int j = 0; j < np; ++j) {
-      const int t0 = __shfl_sync(0xffffffffu, ta, j), t1 = __shfl_sync(0xffffffffu, tb, j);
-      if (t0 > t1) continue;  // warp-uniform
+      const int p0 = __shfl_sync(0xffffffffu, sp.p0, j), p1 = __shfl_sync(0xffffffffu, sp.p1, j);
+      const int n0 = __shfl_sync(0xffffffffu, sp.n0, j), n1 = __shfl_sync(0xffffffffu, sp.n1, j);
+      if (p0 > p1 && n0 > n1) continue;  // warp-uniform
       const float pwx = __shfl_sync(0xffffffffu, wx, j), pwy = __shfl_sync(0xffffffffu, wy, j);
       const float pwz = __shfl_sync(0xffffffffu, wz, j);
       const float pddx = __shfl_sync(0xffffffffu, ddx, j);
       const float pddy = __shfl_sync(0xffffffffu, ddy, j);
       const float pm = __shfl_sync(0xffffffffu, marg, j);
       const float* row = tr + (size_t)(base + j) * g.T;
-      for (int t = t0 + lane; t <= t1; t += 32) {
-        // sample_filtered with the point's constants
-        const float tc = xadd(xmul((float)t, g.bw), g.bo);
-        const float d2 = xsub(xsub(xmul(tc, tc), pddx), pddy);
-        if (!(d2 > 0.f)) continue;
-        Sample sm;
-        const float depth = d2 * rsqrtf(d2);
-        const float zh = fmaf((pwz + depth) - g.oz, g.scale, -0.5f);
-        const float fl = floorf(zh);
-        const float fr = zh - fl;
-        if (!g.exact && fr > pm && fr < 1.f - pm) {
-          if (!(fl >= 0.f && fl + 1.f < (float)g.Z)) continue;
-          sm.zi = (int)fl;
-          sm.alpha = fr;
-          const float q = __fdividef(depth, tc * tc);
-          sm.f2 = (q * q) * (q * q);
-        } else {
-          sm = sample(g, pwx, pwy, pwz, t, x, y);
-          if (!sm.ok) continue;
+      for (int r = 0; r < 2; ++r) {
+        const int t0 = r ? n0 : p0, t1 = r ? n1 : p1;
+        for (int t = t0 + lane; t <= t1; t += 32) {
+          // sample_filtered with the point's constants
+          const float tc = xadd(xmul((float)t, g.bw), g.bo);
+          const float d2 = xsub(xsub(xmul(tc, tc), pddx), pddy);
+          if (!(d2 > 0.f)) continue;
+          Sample sm;
+          const float depth = d2 * rsqrtf(d2);
+          const float zh = fmaf((pwz + depth) - g.oz, g.scale, -0.5f);
+          const float fl = floorf(zh);
+          const float fr = zh - fl;
+          if (!g.exact && fr > pm && fr < 1.f - pm) {
+            if (!(fl >= 0.f && fl + 1.f < (float)g.Z)) continue;
+            sm.zi = (int)fl;
+            sm.alpha = fr;
+            const float q = __fdividef(depth, tc * tc);
+            sm.f2 = (q * q) * (q * q);
+          } else {
+            sm = sample(g, pwx, pwy, pwz, t, x, y);
+            if (!sm.ok) continue;
+          }
+          const float v = __ldg(row + t) * sm.f2;
+          atomicAdd(col + sm.zi, (1.f - sm.alpha) * v);
+          atomicAdd(col + sm.zi + 1, sm.alpha * v);
         }
-        const float v = __ldg(row + t) * sm.f2;
-        atomicAdd(col + sm.zi, (1.f - sm.alpha) * v);
-        atomicAdd(col + sm.zi + 1, sm.alpha * v);
       }
     }
   }
@@ -352,6 +410,272 @@ __global__ void __launch_bounds__(256) confocal_adjoint_kernel(Geo g, Points mp,
     float sum = 0.f;
     for (int w = 0; w < 8; ++w) sum += cols[w * g.Z + z];
     vol[(size_t)c * g.Z + z] = sum;
+  }
+}
+
+// Exact adjoint of the forward without atomics, for columns of at most 32 CPL
+// cells: one CTA per voxel column, each warp over a share of the points (all
+// 32 lanes on the same point), lane l owning the CPL cells z0 = l CPL ..
+// z0 + CPL - 1. A sample whose lower interpolation cell zi is the lane's adds
+// (1 - alpha) v to cell zi and alpha v to cell zi + 1; when zi + 1 is the next
+// lane's first cell that share goes to a per-lane carry register, added in at
+// the end. The samples a lane walks are those of the bins whose centres map to
+// its cells: the bin coordinate of each cell boundary from one square root,
+// widened by eps bins, a bound on the FP32 rounding of the sample chain
+// against that inverse (64 u of the largest magnitudes, over the bin width,
+// plus 0.01, at most the one bin of column_span, inside which the per-point
+// margin holds). Each sample's decisions are the exact chain's (sample_filtered
+// with the per-point margin, as in confocal_adjoint_kernel), so every kept
+// sample is the forward's and each lands in exactly one lane.
+template <int CPL>
+__global__ void __launch_bounds__(256) confocal_adjoint_cells_kernel(Geo g, Points mp, int N,
+                                                                     const float* __restrict__ tr,
+                                                                     float* __restrict__ vol) {
+  __shared__ float cells[8][CPL][32];  // [warp][cell of the lane][lane]
+  __shared__ float carry_in[8][32];
+  const int c = blockIdx.x;
+  const int xi = c / g.Y, yi = c - xi * g.Y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) cells[warp][k][lane] = 0.f;
+  const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
+  const float u = 5.9604645e-8f;
+  const int tz = first_nonneg_bin(g);
+  // this lane's lower cells zi in [za, zb): z in [zlo, zhi)
+  const int za = lane * CPL, zb = min(za + CPL, g.Z - 1);
+  const float zlo = g.oz + ((float)za + 0.5f) / g.scale;
+  const float zhi = g.oz + ((float)zb + 0.5f) / g.scale;
+  float carry = 0.f;
+  for (int base = warp * 32; base < N; base += 256) {
+    // lane j prepares point base + j
+    const int ip = base + lane;
+    float wx = 0.f, wy = 0.f, wz = 0.f, ddx = 0.f, ddy = 0.f, marg = 0.f, eps = 0.f;
+    if (ip < N) {
+      wx = mp.at(0, ip);
+      wy = mp.at(1, ip);
+      wz = mp.at(2, ip);
+      const float dx = xsub(wx, x), dy = xsub(wy, y);
+      ddx = xmul(dx, dx);
+      ddy = xmul(dy, dy);
+      const Spans sp = column_span(g, tz, dx * dx + dy * dy, wz);
+      const float dmax = 1.001f * span_tc_max(g, sp);
+      const float zmax = fabsf(wz) + dmax;
+      const float zhmax = (zmax + fabsf(g.oz)) * g.scale + 0.5f;
+      marg = 8.f * u * g.scale * (dmax + fabsf(wz) + zmax + fabsf(g.oz)) + 4.f * u * zhmax +
+             1e-7f;
+      eps = fminf(64.f * u * (dmax + fabsf(g.bo) + fabsf(wz) + zmax + fabsf(g.oz) +
+                              1.f / g.scale) * g.inv_bw + 0.01f,
+                  1.f);
+    }
+    const int np = min(32, N - base);
+    for (int j = 0; j < np; ++j) {
+      const float pwx = __shfl_sync(0xffffffffu, wx, j), pwy = __shfl_sync(0xffffffffu, wy, j);
+      const float pwz = __shfl_sync(0xffffffffu, wz, j);
+      const float pddx = __shfl_sync(0xffffffffu, ddx, j);
+      const float pddy = __shfl_sync(0xffffffffu, ddy, j);
+      const float pm = __shfl_sync(0xffffffffu, marg, j);
+      const float pe = __shfl_sync(0xffffffffu, eps, j);
+      Spans sp{1, 0, 1, 0};
+      float cl, ch;
+      if (za < zb && tc_bounds(pddx + pddy, pwz, zlo, zhi, cl, ch))
+        sp = tc_spans(g, tz, cl, ch, pe);
+      const float* row = tr + (size_t)(base + j) * g.T;
+      for (int r = 0; r < 2; ++r) {
+        const int t0 = r ? sp.n0 : sp.p0, t1 = r ? sp.n1 : sp.p1;
+        for (int t = t0; t <= t1; ++t) {
+          const float tc = xadd(xmul((float)t, g.bw), g.bo);
+          const float d2 = xsub(xsub(xmul(tc, tc), pddx), pddy);
+          if (!(d2 > 0.f)) continue;
+          int zi;
+          float alpha, f2;
+          const float depth = d2 * rsqrtf(d2);
+          const float zh = fmaf((pwz + depth) - g.oz, g.scale, -0.5f);
+          const float fl = floorf(zh);
+          const float fr = zh - fl;
+          if (!g.exact && fr > pm && fr < 1.f - pm) {
+            if (!(fl >= (float)za && fl < (float)zb)) continue;
+            zi = (int)fl;
+            alpha = fr;
+            const float q = __fdividef(depth, tc * tc);
+            f2 = (q * q) * (q * q);
+          } else {
+            const Sample sm = sample(g, pwx, pwy, pwz, t, x, y);
+            if (!sm.ok || sm.zi < za || sm.zi >= zb) continue;
+            zi = sm.zi;
+            alpha = sm.alpha;
+            f2 = sm.f2;
+          }
+          const float v = __ldg(row + t) * f2;
+          const int k = zi - za;
+          cells[warp][k][lane] += (1.f - alpha) * v;
+          if (k + 1 < CPL) cells[warp][k + 1][lane] += alpha * v;
+          else carry += alpha * v;
+        }
+      }
+    }
+  }
+  carry_in[warp][lane] = carry;
+  __syncthreads();
+  for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
+    const int l = z / CPL, k = z - l * CPL;
+    float sum = 0.f;
+    for (int w = 0; w < 8; ++w) {
+      sum += cells[w][k][l];
+      if (k == 0 && l > 0) sum += carry_in[w][l - 1];
+    }
+    vol[(size_t)c * g.Z + z] = sum;
+  }
+}
+
+// Exact adjoint of the forward with the lanes of a warp over 32 neighbouring
+// voxel columns (an 8 x 4 tile: y fastest) and all lanes on one point and one
+// bin at a time. The point's transient row is then read once per warp (32 bins
+// per coalesced load, handed out by shuffles), and the bin's tc^2 (the sample
+// chain's FP32 value) and 1 / tc^8 come from a per-CTA table in shared memory
+// (broadcast reads), so f2 = (depth / tc^2)^4 = d2^2 / tc^8 needs no second
+// special-function op. Each lane owns its column's cells in shared memory
+// ([cell][lane]: no bank conflicts, no atomics), one copy per warp; the warps
+// of a CTA take interleaved runs of 32 points of one point group, and the CTA
+// adds its summed columns into the volume (which the launcher zeroes) with
+// one atomic per cell when there is more than one group. Two bins per step
+// give each lane two independent sample chains. The bins walked for a point
+// are the union of the lanes' column spans: every valid sample of a lane lies
+// in its own span, and a sample outside it is decided (and rejected) like any
+// other, so each (column, point, bin) is counted once. Decisions are the exact
+// chain's (sample_filtered's margin, taken over the largest |tc| of the union).
+struct AdjSample {
+  int zi;  // lower cell, or -1: no sample
+  float w0, w1;
+};
+
+__device__ __forceinline__ AdjSample adj_sample(const Geo& g, float2 tab, float val, float ddx,
+                                                float ddy, float wz, float pm, float x, float y,
+                                                float wx, float wy, int t) {
+  AdjSample r{-1, 0.f, 0.f};
+  const float d2 = xsub(xsub(tab.x, ddx), ddy);
+  if (!(d2 > 0.f)) return r;
+  const float depth = d2 * rsqrtf(d2);
+  const float zh = fmaf((wz + depth) - g.oz, g.scale, -0.5f);
+  const float fl = floorf(zh);
+  const float fr = zh - fl;
+  float alpha, f2;
+  int zi;
+  if (!g.exact && fabsf(fr - 0.5f) < 0.5f - pm) {
+    zi = (int)fl;  // saturating: out-of-range cells fail the test below
+    if ((unsigned)zi >= (unsigned)(g.Z - 1)) return r;
+    alpha = fr;
+    f2 = (d2 * d2) * tab.y;
+  } else {
+    const Sample sm = sample(g, wx, wy, wz, t, x, y);
+    if (!sm.ok) return r;
+    zi = sm.zi;
+    alpha = sm.alpha;
+    f2 = sm.f2;
+  }
+  const float v = val * f2;
+  r.zi = zi;
+  r.w1 = alpha * v;
+  r.w0 = v - r.w1;
+  return r;
+}
+
+__global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
+    Geo g, Points mp, int N, int points_per_group, const float* __restrict__ tr,
+    float* __restrict__ vol, int accumulate) {
+  extern __shared__ float acc[];  // [warp][Z][32], then the bin table
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float2* tab = reinterpret_cast<float2*>(acc + (size_t)nw * g.Z * 32);  // [T]: tc^2, 1/tc^8
+  const int tiles_y = (g.Y + 7) >> 3;
+  const int ty = (blockIdx.x % tiles_y) * 8, tx = (blockIdx.x / tiles_y) * 4;
+  const int yi = ty + (lane & 7), xi = tx + (lane >> 3);
+  const bool live = xi < g.X && yi < g.Y;
+  for (int j = threadIdx.x; j < nw * g.Z * 32; j += blockDim.x) acc[j] = 0.f;
+  for (int t = threadIdx.x; t < g.T; t += blockDim.x) {
+    const float tc = xadd(xmul((float)t, g.bw), g.bo);
+    const float tc2 = xmul(tc, tc);
+    const float i2 = __fdividef(1.f, tc2);
+    tab[t] = make_float2(tc2, (i2 * i2) * (i2 * i2));
+  }
+  __syncthreads();
+  float* col = acc + (size_t)warp * g.Z * 32 + lane;
+  const float x = centre(g.ox, g.sx, g.X, live ? xi : 0);
+  const float y = centre(g.oy, g.sy, g.Y, live ? yi : 0);
+  const float u = 5.9604645e-8f;
+  const int tz = first_nonneg_bin(g);
+  const int i0 = blockIdx.y * points_per_group;
+  const int i1 = min(N, i0 + points_per_group);
+  for (int base = i0 + warp * 32; base < i1; base += nw * 32) {
+    // lane j loads point base + j
+    const int ip = base + lane;
+    float lwx = 0.f, lwy = 0.f, lwz = 0.f;
+    if (ip < i1) {
+      lwx = mp.at(0, ip);
+      lwy = mp.at(1, ip);
+      lwz = mp.at(2, ip);
+    }
+    const int np = min(32, i1 - base);
+    for (int j = 0; j < np; ++j) {
+      const float wx = __shfl_sync(0xffffffffu, lwx, j);
+      const float wy = __shfl_sync(0xffffffffu, lwy, j);
+      const float wz = __shfl_sync(0xffffffffu, lwz, j);
+      const float dx = xsub(wx, x), dy = xsub(wy, y);
+      const float ddx = live ? xmul(dx, dx) : INFINITY, ddy = live ? xmul(dy, dy) : 0.f;
+      Spans sp{1, 0, 1, 0};
+      if (live) sp = column_span(g, tz, dx * dx + dy * dy, wz);
+      // warp union of the lanes' spans
+      const int p0 = __reduce_min_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p0 : INT_MAX);
+      const int p1 = __reduce_max_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p1 : -1);
+      int n0 = INT_MAX, n1 = -1;
+      if (tz > 0) {  // warp-uniform
+        n0 = __reduce_min_sync(0xffffffffu, sp.n0 <= sp.n1 ? sp.n0 : INT_MAX);
+        n1 = __reduce_max_sync(0xffffffffu, sp.n0 <= sp.n1 ? sp.n1 : -1);
+      }
+      if (p0 > p1 && n0 > n1) continue;  // warp-uniform
+      const Spans un{p0, p1, n0, n1};
+      // sample_filtered's margin over the union's largest |tc| (warp-uniform)
+      const float dmax = 1.001f * span_tc_max(g, un);
+      const float zmax = fabsf(wz) + dmax;
+      const float zhmax = (zmax + fabsf(g.oz)) * g.scale + 0.5f;
+      const float pm = 8.f * u * g.scale * (dmax + fabsf(wz) + zmax + fabsf(g.oz)) +
+                       4.f * u * zhmax + 1e-7f;
+      const float* row = tr + (size_t)(base + j) * g.T;
+      for (int r = 0; r < 2; ++r) {
+        const int t0 = r ? n0 : p0, t1 = r ? n1 : p1;
+        float wval = 0.f;  // bin t0 + 32 k + lane
+        for (int t = t0; t <= t1; t += 2) {
+          const int wo = (t - t0) & 31;
+          if (wo == 0) wval = t + lane <= t1 ? __ldg(row + t + lane) : 0.f;
+          const float va = __shfl_sync(0xffffffffu, wval, wo);
+          const float vb = __shfl_sync(0xffffffffu, wval, wo + 1);
+          const bool has_b = t + 1 <= t1;  // warp-uniform
+          const AdjSample a = adj_sample(g, tab[t], va, ddx, ddy, wz, pm, x, y, wx, wy, t);
+          AdjSample bs{-1, 0.f, 0.f};
+          if (has_b)
+            bs = adj_sample(g, tab[t + 1], vb, ddx, ddy, wz, pm, x, y, wx, wy, t + 1);
+          if (a.zi >= 0) {
+            col[a.zi * 32] += a.w0;
+            col[a.zi * 32 + 32] += a.w1;
+          }
+          if (bs.zi >= 0) {
+            col[bs.zi * 32] += bs.w0;
+            col[bs.zi * 32 + 32] += bs.w1;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // cell z of column l: the sum over the warps' copies (l fastest: no bank
+  // conflicts in the reads)
+  for (int jj = threadIdx.x; jj < g.Z * 32; jj += blockDim.x) {
+    const int z = jj >> 5, l = jj & 31;
+    const int cy = ty + (l & 7), cx = tx + (l >> 3);
+    if (cx >= g.X || cy >= g.Y) continue;
+    float sum = 0.f;
+    for (int w = 0; w < nw; ++w) sum += acc[((size_t)w * g.Z + z) * 32 + l];
+    float* dst = vol + ((size_t)cx * g.Y + cy) * g.Z + z;
+    if (accumulate) atomicAdd(dst, sum);
+    else *dst = sum;
   }
 }
 
@@ -429,8 +753,11 @@ Geo make_geo(int X, int Y, int Z, const float* o, const float* s, float bw, floa
   g.scale = (float)Z / s[2];
   g.bw = bw;
   g.bo = bo;
+  g.inv_bw = 1.f / bw;
   g.T = T;
   g.exact = tune::get("volume.exact") == 1;
+  g.all_bins = !(bw > 0.f) || !std::isfinite(bw) || !std::isfinite(bo) ||
+               !std::isfinite(g.inv_bw);
   return g;
 }
 
@@ -509,13 +836,64 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
     return TOTRI_OK;
   }
   const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
+  const unsigned grid = (unsigned)(X * Y);
+  const float* trd = static_cast<const float*>(tr->data);
+  float* vd = static_cast<float*>(vol->data);
+  // "volume.adjoint.mode": 0 (default) lanes over columns, 1 shared-memory
+  // atomics, 2 lane-owned cells (columns of up to 256 cells)
+  const int mode = tune::get("volume.adjoint.mode");
+  // lanes over columns: warps per CTA such that two CTAs' copies of 32
+  // columns and the bin table fit an SM's shared memory
+  // ("volume.adjoint.warps" overrides); bins beyond 4,096 take the atomic kernel
+  const size_t table = sizeof(float2) * (size_t)T;
+  const size_t per_warp = (size_t)Z * 32 * sizeof(float);
+  int warps = T <= 4096 && table < 113 * 1024 ? (int)((113 * 1024 - table) / per_warp) : 0;
+  if (tune::get("volume.adjoint.warps") > 0) warps = tune::get("volume.adjoint.warps");
+  warps = std::min(warps, 8);
+  if (mode == 0 && warps >= 1 && T <= 4096) {
+    const size_t smem = (size_t)warps * per_warp + table;
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(volume::confocal_adjoint_columns_kernel), smem));
+    const int64_t tiles = ceil_div(Y, 8) * ceil_div(X, 4);
+    // point groups: about 16 CTAs per SM in all, each group at least four
+    // runs of 32 points per warp
+    const int64_t want = std::max<int64_t>(1, (16 * tune::sm_count()) / tiles);
+    const int groups =
+        (int)std::max<int64_t>(1, std::min<int64_t>(want, N / (128 * warps)));
+    const int per = (int)(ceil_div(ceil_div(N, groups), 32) * 32);
+    const int used = (int)ceil_div(N, per);
+    if (used > 1) TOTRI_CUDA(cudaMemsetAsync(vd, 0, sizeof(float) * numel(vol), stream));
+    TOTRI_KERNEL("volume confocal adjoint", stream,
+                 volume::confocal_adjoint_columns_kernel<<<dim3((unsigned)tiles, (unsigned)used),
+                                                           warps * 32, smem, stream>>>(
+                     g, pts, N, per, trd, vd, used > 1 ? 1 : 0));
+    return TOTRI_OK;
+  }
+  if (Z <= 256 && mode == 2) {
+    if (Z <= 32)
+      TOTRI_KERNEL("volume confocal adjoint", stream,
+                   volume::confocal_adjoint_cells_kernel<1><<<grid, 256, 0, stream>>>(
+                       g, pts, N, trd, vd));
+    else if (Z <= 64)
+      TOTRI_KERNEL("volume confocal adjoint", stream,
+                   volume::confocal_adjoint_cells_kernel<2><<<grid, 256, 0, stream>>>(
+                       g, pts, N, trd, vd));
+    else if (Z <= 128)
+      TOTRI_KERNEL("volume confocal adjoint", stream,
+                   volume::confocal_adjoint_cells_kernel<4><<<grid, 256, 0, stream>>>(
+                       g, pts, N, trd, vd));
+    else
+      TOTRI_KERNEL("volume confocal adjoint", stream,
+                   volume::confocal_adjoint_cells_kernel<8><<<grid, 256, 0, stream>>>(
+                       g, pts, N, trd, vd));
+    return TOTRI_OK;
+  }
   const size_t smem = sizeof(float) * 8 * (size_t)Z;
   if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "volume too deep for one column tile");
   TOTRI_CUDA(tune::ensure_dynamic_smem(
       reinterpret_cast<const void*>(volume::confocal_adjoint_kernel), smem));
   TOTRI_KERNEL("volume confocal adjoint", stream,
-               volume::confocal_adjoint_kernel<<<(unsigned)(X * Y), 256, smem, stream>>>(
-                   g, pts, N, static_cast<const float*>(tr->data), static_cast<float*>(vol->data)));
+               volume::confocal_adjoint_kernel<<<grid, 256, smem, stream>>>(g, pts, N, trd, vd));
   return TOTRI_OK;
 }
 

@@ -157,7 +157,11 @@ class RbfFitting:
                  laser_origin: typing.Optional[torch.Tensor] = None,
                  optimize_check_delete: bool = False, delete_Factor: float = 1.001,
                  tensorboard: bool = False, video: bool = False, log_dir: str = None,
-                 project_transient: bool = True):
+                 project_transient: bool = True,
+                 generator: typing.Optional[torch.Generator] = None):
+        """generator: the random source of the blob moves (volume and surface
+        samples, split choices and offsets), on the device of the scan points;
+        torch's default generator when None."""
         if tensorboard or video:
             raise NotImplementedError("TensorBoard and video output are not part of totri_gb300")
         self.bin_def_init = bin_def
@@ -168,6 +172,7 @@ class RbfFitting:
         self.delete_Factor = delete_Factor
         self.project_transient = project_transient
         self.log_dir = log_dir
+        self.generator = generator
 
     def reduce_transient(self, transient_input, margin=32):
         """Crops leading and trailing bins without signal (rbf.py:218-243):
@@ -314,7 +319,8 @@ class RbfFitting:
                                                       b(self.scan_origin), b(self.laser_origin))
         ve = second_derivative_filter(ve.clamp(min=0))
         ve = (ve / ve.max()) ** 2
-        samples = torch.multinomial(ve.flatten(), num_samples, replacement=False).tolist()
+        samples = torch.multinomial(ve.flatten(), num_samples, replacement=False,
+                                    generator=self.generator).tolist()
         base_new, bg_new = base.clone(), background_model.clone()
         for smp in samples:
             x, y, z = vd.index_to_coordinates(vd.flat_idx_to_3d_idx(smp))
@@ -335,7 +341,8 @@ class RbfFitting:
         w = (verts.grad ** 2).sum(dim=-1) ** 0.5
         if float(w.sum()) == 0:
             return []
-        idx = torch.multinomial(w, min(num_samples, verts.shape[0]), replacement=False)
+        idx = torch.multinomial(w, min(num_samples, verts.shape[0]), replacement=False,
+                                generator=self.generator)
         return verts.detach()[idx].tolist()
 
     def add_blobs_surface(self, base, background_model, transient_input, num_samples=5):
@@ -359,11 +366,13 @@ class RbfFitting:
         new = min(min(32, n), max(0, 500 - n))
         base_new, bg_new = base.clone(), background_model.clone()
         if new > 0:
-            for idx in torch.multinomial(base.get_sigma()[:, 0], new, replacement=False).tolist():
+            picks = torch.multinomial(base.get_sigma()[:, 0], new, replacement=False,
+                                      generator=self.generator).tolist()
+            for idx in picks:
                 base_new.params[idx, 3] = 0.75 * base_new.params[idx, 3]
                 base_new.params = torch.cat((base_new.params, base_new.params[None, idx]), 0)
-                off = base_new.params[idx, 3] * (2 * torch.rand((2,), device=base.params.device)
-                                                 - 1)
+                off = base_new.params[idx, 3] * (2 * torch.rand((2,), device=base.params.device,
+                                                                generator=self.generator) - 1)
                 base_new.params[idx, :2] += off
                 base_new.params[-1, :2] -= off
         _, final, _ = self.optimize(base_new, bg_new, transient_input, num_iter=400)

@@ -37,6 +37,21 @@ Kinds (``Request.kind``):
                     early stop): (translation [3], quaternion [4], losses
                     [iterations]). The pose changes the geometry every step,
                     so each step rebuilds the BVH and masks in its own scratch.
+  * "fit_depth_map" — ``iterations`` steps of the depth-map fit
+                    (``fitting.DepthMapFitting`` with its default weights and
+                    learning-rate schedule) of a height field over ``volume``
+                    (resolution (D, H, W): an H x W grid) to measurement
+                    ``target``: (depth [H, W], albedo [H, W], losses
+                    [iterations]). Enqueued like fit_pose, without host
+                    synchronisation.
+  * "fit_rbf"     — ``iterations`` driver moves of the Gaussian-blob fit
+                    (``fitting.RbfFitting``: add, split, delete, refine) from an
+                    empty set of blobs in ``volume`` to measurement ``target``,
+                    its random choices drawn from a generator seeded with
+                    ``seed``: (blobs [n, 4] as x, y, z, sigma, data loss). The
+                    moves accept or reject on the host, so the fit runs on a
+                    worker thread with the request's stream current; it always
+                    counts as large.
 """
 import collections
 import concurrent.futures
@@ -62,6 +77,7 @@ class Request:
     target: typing.Optional[str] = None
     volume: typing.Optional[VolumeDef] = None
     iterations: int = 0
+    seed: int = 0
     # filled in by the server
     id: int = -1
     arrival: float = 0.0
@@ -136,6 +152,35 @@ class MaskCache:
             e = self.entries.pop(key)
             self.budget.resident -= e.nbytes
         return self.budget.fits(need)
+
+
+class _Threaded:
+    """A request run on a host thread (it needs host decisions between its
+    kernels) with its slot's stream current on that thread. ``query()`` is
+    True once the thread has returned and the copies it enqueued last have
+    completed; ``result`` or ``exc`` then holds the outcome."""
+
+    def __init__(self, fn, stream, device):
+        self.result, self.exc, self.event = None, None, None
+        self._stream, self._device = stream, device
+        self.thread = threading.Thread(target=self._run, args=(fn,), daemon=True)
+        self.thread.start()
+
+    def _run(self, fn):
+        try:
+            torch.cuda.set_device(self._device)
+            with torch.cuda.stream(self._stream):
+                self.result = fn()
+                ev = torch.cuda.Event()
+                ev.record(self._stream)
+                self.event = ev
+        except BaseException as exc:  # reported through the request's future
+            self.exc = exc
+
+    def query(self):
+        if self.thread.is_alive():
+            return False
+        return self.event is None or self.event.query()
 
 
 class _Mesh:
@@ -227,30 +272,35 @@ class Server:
             self.cv.notify()
         return fut
 
+    KINDS = ("render", "grad", "backproject", "fit_pose", "fit_depth_map", "fit_rbf")
+    _FITS = ("fit_pose", "fit_depth_map", "fit_rbf")
+
     def _validate(self, r):
+        if r.kind not in self.KINDS:
+            raise ValueError("unknown request kind %r" % r.kind)
         if r.grid not in self.grids:
             raise KeyError("unknown grid %r" % r.grid)
         if r.kind in ("render", "grad", "fit_pose"):
             if r.mesh not in self.meshes:
                 raise KeyError("unknown mesh %r" % r.mesh)
-            if r.bins is None:
-                raise ValueError("render/grad/fit_pose requests need bins")
-        if r.kind == "fit_pose" and r.iterations < 1:
-            raise ValueError("fit_pose requests need iterations >= 1")
-        if r.kind in ("grad", "backproject", "fit_pose"):
+        if r.kind in ("render", "grad") + self._FITS and r.bins is None:
+            raise ValueError("%s requests need bins" % r.kind)
+        if r.kind in self._FITS and r.iterations < 1:
+            raise ValueError("%s requests need iterations >= 1" % r.kind)
+        if r.kind != "render":
             if r.target not in self.measurements:
                 raise KeyError("unknown measurement %r" % r.target)
             tr, grid, bins = self.measurements[r.target]
             if grid != r.grid:
                 raise ValueError("measurement %r is on grid %r" % (r.target, grid))
-            if r.kind in ("grad", "fit_pose") and (bins.num, bins.width, bins.offset) != (
+            if r.kind != "backproject" and (bins.num, bins.width, bins.offset) != (
                     r.bins.num, r.bins.width, r.bins.offset):
                 raise ValueError("measurement %r is binned differently from the request"
                                  % r.target)
-        if r.kind == "backproject" and r.volume is None:
-            raise ValueError("backproject requests need a VolumeDef")
-        if r.kind not in ("render", "grad", "backproject", "fit_pose"):
-            raise ValueError("unknown request kind %r" % r.kind)
+        if r.kind in ("backproject", "fit_depth_map", "fit_rbf") and r.volume is None:
+            raise ValueError("%s requests need a VolumeDef" % r.kind)
+        if r.kind == "fit_depth_map" and min(r.volume.resolution[1:]) < 2:
+            raise ValueError("fit_depth_map needs a grid of at least 2 x 2")
 
     # Rates behind cost_ms, measured on one GB300 (the differentiable
     # 20,480-face workload and the 128^3 Velten backprojection): visibility
@@ -268,6 +318,14 @@ class Server:
             for n in r.volume.resolution:
                 vox *= int(n)
             return 1e3 * (vox * S / k["backproject"] + 4 * vox / k["copy"])
+        if r.kind == "fit_depth_map":
+            V, F = self._depth_map_size(r)
+            return 1e3 * r.iterations * F * S * (1 / k["visibility"] + 1 / k["splat"] +
+                                                 1 / k["grad"])
+        if r.kind == "fit_rbf":  # each driver move runs hundreds of optimiser steps
+            V, F = self._rbf_mesh_bound(r)
+            return 1e3 * r.iterations * 300 * F * S * (1 / k["visibility"] + 1 / k["splat"] +
+                                                       1 / k["grad"])
         m = self.meshes[r.mesh]
         pairs = m.F * S
         if r.kind == "fit_pose":
@@ -282,6 +340,21 @@ class Server:
             sec += pairs / k["visibility"]
         return 1e3 * sec
 
+    @staticmethod
+    def _depth_map_size(r):
+        """(vertices, faces) of a depth-map request's H x W grid."""
+        H, W = int(r.volume.resolution[1]), int(r.volume.resolution[2])
+        return H * W, 2 * (H - 1) * (W - 1)
+
+    @staticmethod
+    def _rbf_mesh_bound(r):
+        """A planning bound on the (vertices, faces) of the iso-surface of an RBF
+        fit's volume (its size is only known as the fit runs): eight faces per
+        cell of the three axis-aligned mid-sections."""
+        D, H, W = (int(n) for n in r.volume.resolution)
+        F = 8 * (D * H + H * W + W * D)
+        return 3 * F, F
+
     def _mask_bytes(self, r):
         S = self.grids[r.grid].shape[1]
         return int(self.lib.totri_mesh_mask_bytes(1, self.meshes[r.mesh].F, S))
@@ -292,6 +365,17 @@ class Server:
         S = self.grids[r.grid].shape[1]
         if r.kind == "backproject":
             return 4 * int(torch.tensor(r.volume.resolution).prod())
+        if r.kind in ("fit_depth_map", "fit_rbf"):
+            # per step: scratch with masks, transients and their gradients,
+            # parameters with gradients and optimiser state (and the RBF volume)
+            V, F = (self._depth_map_size(r) if r.kind == "fit_depth_map"
+                    else self._rbf_mesh_bound(r))
+            ws = int(self.lib.totri_mesh_workspace(1, V, F, S))
+            need = ws + 4 * 4 * r.bins.num * S + 32 * 4 * V
+            if r.kind == "fit_rbf":
+                D, H, W = (int(n) for n in r.volume.resolution)
+                need += 64 * D * H * W
+            return need
         m = self.meshes[r.mesh]
         if r.kind == "fit_pose":  # per step: scratch with masks, two transients, gradients
             ws = int(self.lib.totri_mesh_workspace(1, m.verts.shape[1], m.F, S))
@@ -315,6 +399,10 @@ class Server:
         key = None
         if r.kind == "fit_pose":
             return self._fit_pose(r)
+        if r.kind == "fit_depth_map":
+            return self._fit_depth_map(r)
+        if r.kind == "fit_rbf":
+            return _Threaded(lambda: self._fit_rbf(r), stream, self.device)
         if r.kind in ("render", "grad"):
             m = self.meshes[r.mesh]
             key = (r.mesh, r.grid)
@@ -391,6 +479,44 @@ class Server:
         out[2].copy_(losses, non_blocking=True)
         return out
 
+    def _fit_depth_map(self, r):
+        """Enqueues the depth-map fit on the current stream; no host
+        synchronisation."""
+        from .fitting import DepthMap, DepthMapFitting
+        target = self.measurements[r.target][0]
+        target.record_stream(torch.cuda.current_stream(self.device))
+        vd = VolumeDef(r.volume.start, r.volume.end, r.volume.resolution)
+        dm = DepthMap(vd, device=self.device)
+        fitting = DepthMapFitting(r.bins)
+        fitting.fit(dm, target[0], self.grids[r.grid][0], num_iter=r.iterations)
+        losses = torch.stack(fitting.losses)
+        out = (torch.empty(dm.depth.shape, dtype=torch.float32, pin_memory=True),
+               torch.empty(dm.color.shape, dtype=torch.float32, pin_memory=True),
+               torch.empty(r.iterations, dtype=torch.float32, pin_memory=True))
+        out[0].copy_(dm.depth.detach(), non_blocking=True)
+        out[1].copy_(dm.color.detach(), non_blocking=True)
+        out[2].copy_(losses, non_blocking=True)
+        return out
+
+    def _fit_rbf(self, r):
+        """The Gaussian-blob fit; runs on a worker thread (see _Threaded)."""
+        from .fitting import GaussianRbfBase, RbfFitting, TransientBackgroundEmpty
+        target = self.measurements[r.target][0][0]
+        target.record_stream(torch.cuda.current_stream(self.device))
+        gen = torch.Generator(device=self.device)
+        gen.manual_seed(int(r.seed))
+        vd = VolumeDef(r.volume.start, r.volume.end, r.volume.resolution)
+        fitting = RbfFitting(r.bins, self.grids[r.grid][0], generator=gen)
+        base = fitting.fit(GaussianRbfBase(vd, device=self.device), target,
+                           num_iter=r.iterations)
+        norm = target / target.mean()
+        loss = fitting.loss_all(base, TransientBackgroundEmpty(), norm)[0]["data"]
+        out = (torch.empty(base.params.shape, dtype=torch.float32, pin_memory=True),
+               torch.empty((), dtype=torch.float32, pin_memory=True))
+        out[0].copy_(base.params.detach(), non_blocking=True)
+        out[1].copy_(loss.detach(), non_blocking=True)
+        return out
+
     def _admit_one(self):
         """Admits the first of the next `lookahead` queued requests that fits
         and has a free stream of its class; drops cancelled ones."""
@@ -404,7 +530,7 @@ class Server:
             if fut.cancelled():
                 del self.queue[qi]
                 return True
-            large = self.cost_ms(r) >= self.large_ms
+            large = r.kind == "fit_rbf" or self.cost_ms(r) >= self.large_ms
             slots = [i for i in free if self.slot_large[i] == large]
             if not slots:
                 continue
@@ -428,8 +554,11 @@ class Server:
             try:
                 with torch.cuda.stream(stream):
                     result = self._launch(r, stream)
-                    ev = torch.cuda.Event()
-                    ev.record(stream)
+                    if isinstance(result, _Threaded):
+                        ev = result  # done when its thread and last copies are
+                    else:
+                        ev = torch.cuda.Event()
+                        ev.record(stream)
             except Exception as exc:  # invalid request data: fail this request only
                 if new_mask and key in self.masks.entries:
                     need -= self._mask_bytes(r)  # cached before the failure: now resident
@@ -459,6 +588,12 @@ class Server:
             if r.kind in ("render", "grad"):
                 self.masks.unpin((r.mesh, r.grid))
             r.done = time.perf_counter()
+            if isinstance(result, _Threaded):
+                exc, result = result.exc, result.result
+                if exc is not None and not fut.cancelled():
+                    fut.set_exception(exc)
+                    done = True
+                    continue
             if fut.cancelled():  # cancelled in flight: the result is dropped
                 self.cancelled += 1
             else:
