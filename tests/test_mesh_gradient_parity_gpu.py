@@ -215,7 +215,9 @@ def exhaustive_large(cuda_lib):
     return dict(n=n, d=d, bd=bd, ref=ref, tg=torch.from_numpy(tg)[None].cuda(), rv=rv, rm=rm)
 
 
-_SPLAT_VARIANTS = [{}, {"mesh.exhaustive.splat.occupancy": 1}]
+_SPLAT_VARIANTS = [{}, {"mesh.exhaustive.splat.occupancy": 1},
+                   {"mesh.exhaustive.splat.cluster": 1},
+                   {"mesh.exhaustive.splat.occupancy": 1, "mesh.exhaustive.splat.cluster": 1}]
 
 
 @pytest.mark.parametrize("keys", _SPLAT_VARIANTS, ids=lambda k: ",".join(
@@ -223,7 +225,9 @@ _SPLAT_VARIANTS = [{}, {"mesh.exhaustive.splat.occupancy": 1}]
 @pytest.mark.parametrize("lt", autotune.CANDIDATES["mesh.exhaustive.splat.lt"])
 def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt, keys):
     """Every laser tile, with the register-capped splat (the default) or the
-    uncapped one ("mesh.exhaustive.splat.occupancy" = 1)."""
+    uncapped one ("mesh.exhaustive.splat.occupancy" = 1), and for tiles
+    narrower than 8 lasers with the cluster flush (the default) or each tile
+    flushing alone ("mesh.exhaustive.splat.cluster" = 1)."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]
     empty = torch.empty_like(d["sp"][:, :0])
@@ -251,7 +255,8 @@ def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt, keys
 
 _GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.mode": 2},
                   {"mesh.exhaustive.grad.occupancy": 4}, {"mesh.exhaustive.grad.faces": 1},
-                  {"mesh.exhaustive.grad.faces": 5}, {"mesh.exhaustive.grad.faces": 32}]
+                  {"mesh.exhaustive.grad.faces": 5}, {"mesh.exhaustive.grad.faces": 32},
+                  {"mesh.exhaustive.grad.lchunk": 5}, {"mesh.exhaustive.grad.lchunk": 8}]
 
 
 @pytest.mark.parametrize("keys", _GRAD_VARIANTS, ids=lambda k: ",".join(
@@ -259,8 +264,8 @@ _GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.m
 def test_exhaustive_large_gradient_matches_fp64_oracle(exhaustive_large, keys):
     """The three gradient kernels (separable point records, the default;
     per-lane mask tests; compacted triples) and the point-record kernel's
-    register cap and faces-per-CTA shapes (including counts that do not
-    divide the face count) against the FP64 oracle."""
+    register cap, faces-per-CTA and laser-chunk shapes (including counts that
+    do not divide the face or laser count) against the FP64 oracle."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]
     empty = torch.empty_like(d["sp"][:, :0])

@@ -11,10 +11,14 @@
 // points with a [T][tile] shared histogram flushed as rows of the [T][S][L]
 // output; the gradient gives each CTA 32 faces and a slice of scan points and
 // walks every (s, l) pair of the slice.
+#include <cooperative_groups.h>
+
 #include "capi_common.cuh"
 #include "mesh.cuh"
 #include "mesh_kernels.cuh"
 #include "tune.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace totri {
 namespace mesh {
@@ -118,7 +122,14 @@ __device__ __forceinline__ float origin_term(const Origins& o, int b, int s, int
   return od;
 }
 
-template <int LT, int kOcc = 1>
+// One CTA per (scan point, tile of LT lasers): the tile's [T][LT] histogram in
+// shared memory, flushed once. With CL > 1 the CTAs of a cluster of CL
+// neighbouring tiles (CL LT = 8 lasers) each flush every CL-th bin row for the
+// whole cluster, reading the other tiles' histograms through distributed
+// shared memory, so every row piece is one full 32-byte sector: a 4-laser
+// tile's own 16-byte pieces make the memory read, merge and write back each
+// sector (8.75 GB of DRAM traffic for a 2 GB transient).
+template <int LT, int kOcc = 1, int CL = 1>
 __global__ void __launch_bounds__(256, kOcc) exh_splat_kernel(Scene sc, View3f sp, View3f lp, Origins org,
                                                         int S, int L, float* __restrict__ out,
                                                         int T, float bw, float bo, FastBins fb) {
@@ -152,11 +163,27 @@ __global__ void __launch_bounds__(256, kOcc) exh_splat_kernel(Scene sc, View3f s
     }
   }
   __syncthreads();
-  // rows out[b][t][s][l0 .. l0+LT)
-  float* ob = out + (((size_t)b * T) * S + s) * L + l0;
-  for (int i = threadIdx.x; i < T * LT; i += blockDim.x) {
-    const int t = i / LT, c = i - t * LT;
-    if (l0 + c < L) ob[(size_t)t * S * L + c] = hist[i];
+  if (CL == 1) {
+    // rows out[b][t][s][l0 .. l0+LT)
+    float* ob = out + (((size_t)b * T) * S + s) * L + l0;
+    for (int i = threadIdx.x; i < T * LT; i += blockDim.x) {
+      const int t = i / LT, c = i - t * LT;
+      if (l0 + c < L) ob[(size_t)t * S * L + c] = hist[i];
+    }
+  } else {
+    cg::cluster_group cluster = cg::this_cluster();
+    cluster.sync();  // every tile of the cluster has its histogram
+    const int rank = (int)cluster.block_rank();
+    const int L0 = l0 - rank * LT;  // the cluster's first laser
+    float* ob = out + (((size_t)b * T) * S + s) * L + L0;
+    const int rows = (T - rank + CL - 1) / CL;
+    for (int i = threadIdx.x; i < rows * CL * LT; i += blockDim.x) {
+      const int t = rank + CL * (i / (CL * LT)), j = i % (CL * LT);
+      const int src = j / LT, c = j - src * LT;
+      const float* rh = cluster.map_shared_rank(hist, src);
+      if (L0 + j < L) ob[(size_t)t * S * L + j] = rh[t * LT + c];
+    }
+    cluster.sync();  // no tile leaves while another still reads its histogram
   }
 }
 
@@ -551,7 +578,7 @@ __device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* tota
 template <int kOcc>
 __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
     Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
-    int T, float bw, float bo, GradOut out, int faces_per_cta) {
+    int T, float bw, float bo, GradOut out, int faces_per_cta, int lchunk) {
   extern __shared__ float recs[];        // scan-point then laser-point records, SoA
   float* srec = recs;
   float* lrec = recs + kRec * kFaceSlice;
@@ -560,8 +587,10 @@ __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
   __shared__ float red[8][10];
   const int b = blockIdx.y;
   const int n = sc.meta[b].n;
-  const int s0 = blockIdx.z * kFaceSlice;
+  const int nlc = (L + lchunk - 1) / lchunk;
+  const int s0 = (blockIdx.z / nlc) * kFaceSlice;
   const int ns_all = min(kFaceSlice, S - s0);
+  const int la = (blockIdx.z % nlc) * lchunk, lb = min(L, la + lchunk);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float* tgb = tgrad + (size_t)b * T * S * L;
   const int64_t stride = (int64_t)S * L;
@@ -600,11 +629,12 @@ __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.f;
-    for (int l0 = 0; l0 < L && ns > 0; l0 += kFaceSlice) {
+    for (int l0 = la; l0 < lb && ns > 0; l0 += kFaceSlice) {
       int nl;
       {
         const int l = l0 + tid;
-        const bool vis = l < L && (mrows[(size_t)(S + l) * sc.nch + ch] & bit);
+        const bool vis = l < lb && tid < kFaceSlice &&
+                         (mrows[(size_t)(S + l) * sc.nch + ch] & bit);
         const int at = block_slot(vis, counts[1], &nl);
         if (vis) {
           const fv3 p = mkv(lp.at(b, l, 0), lp.at(b, l, 1), lp.at(b, l, 2));
@@ -754,6 +784,32 @@ static int launch_exh_splat(const Scene& sc, const View3f& sp, const View3f& lp,
   // detector x 16x16 laser points) they took 4.4 s against 4.9 s for the
   // compacted variant, which "mesh.exhaustive.splat.mode" = 1 selects.
   if (tune::get("mesh.exhaustive.splat.mode") != 1) {
+    // Tiles narrower than a 32-byte sector flush through a cluster of
+    // 8 / LT tiles ("mesh.exhaustive.splat.cluster" = 1: each tile alone).
+    constexpr int CL = LT < 8 ? 8 / LT : 1;
+    if (CL > 1 && tune::get("mesh.exhaustive.splat.cluster") != 1) {
+      const bool capped = tune::get("mesh.exhaustive.splat.occupancy") != 1;
+      auto* kern = capped ? exh_splat_kernel<LT, 5, CL> : exh_splat_kernel<LT, 1, CL>;
+      TOTRI_CUDA(tune::ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid.x, (unsigned)(ceil_div(grid.y, CL) * CL), grid.z);
+      cfg.blockDim = dim3(256);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 1;
+      attr[0].val.clusterDim.y = CL;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      cudaError_t le = cudaSuccess;
+      TOTRI_KERNEL("mesh exhaustive splat", stream,
+                   le = cudaLaunchKernelEx(&cfg, kern, sc, sp, lp, org, S, L, out, T, bw, bo,
+                                           fast));
+      TOTRI_CUDA(le);
+      return TOTRI_OK;
+    }
     // Registers capped for 5 CTAs per SM (48, no spills): 36.5 ms against
     // 38.1 ms uncapped (58 registers; "mesh.exhaustive.splat.occupancy" = 1)
     // on one 20k-face mesh, 32x32 x 16x16 points, 2,048 bins.
@@ -834,25 +890,32 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   if (mode != 1 && mode != 2) {
     // "mesh.exhaustive.grad.faces": faces per CTA (default 8);
     // "mesh.exhaustive.grad.occupancy" = 4: registers capped for 4 CTAs per SM
-    // (64, with spills) instead of 3 (80)
+    // (64, with spills) instead of 3 (80). Lasers are split into chunks of
+    // `lchunk` per CTA, faces varying fastest over the grid, so the CTAs that
+    // run together read the transient_grad rows of one (scan slice, laser
+    // chunk): at 64x64 x 16x16 points that footprint no longer fits L2 with
+    // all 256 lasers per CTA (0.37 against 0.23 ms per thousand pairs at
+    // 64x64 x 8x8). "mesh.exhaustive.grad.lchunk" overrides.
     const int fpc = tune::get("mesh.exhaustive.grad.faces") > 0
                         ? (int)tune::get("mesh.exhaustive.grad.faces")
                         : kFacesPerCta;
+    int lchunk = tune::get("mesh.exhaustive.grad.lchunk");
+    if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = kFaceSlice;
     const bool occ4 = tune::get("mesh.exhaustive.grad.occupancy") == 4;
     const void* fn = occ4 ? reinterpret_cast<const void*>(exh_grad_face_kernel<4>)
                           : reinterpret_cast<const void*>(exh_grad_face_kernel<3>);
     const size_t smem = sizeof(float) * 2 * kRec * kFaceSlice;
     TOTRI_CUDA(tune::ensure_dynamic_smem(fn, smem));
     const dim3 grid((unsigned)ceil_div(sc.F, fpc), (unsigned)sc.B,
-                    (unsigned)ceil_div(S, kFaceSlice));
+                    (unsigned)(ceil_div(S, kFaceSlice) * ceil_div(L, lchunk)));
     if (occ4)
       TOTRI_KERNEL("mesh exhaustive grad", stream,
                    exh_grad_face_kernel<4><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc));
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk));
     else
       TOTRI_KERNEL("mesh exhaustive grad", stream,
                    exh_grad_face_kernel<3><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc));
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk));
     return TOTRI_OK;
   }
   if (mode == 1) {

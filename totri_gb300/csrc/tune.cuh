@@ -7,12 +7,15 @@
 //   "mesh.exhaustive.splat.lt"  laser points per exhaustive splat CTA (1,4,8,16,32)
 //   "mesh.exhaustive.splat.mode", "mesh.exhaustive.splat.occupancy"
 //                               exhaustive splat variant / 1: uncapped registers
+//   "mesh.exhaustive.splat.cluster" 1: tiles under 8 lasers flush alone (default:
+//                               through a cluster, in whole 32-byte sectors)
 //   "mesh.exhaustive.exact"     1: every exhaustive sample takes the exact chain
 //   "mesh.exhaustive.grad.mode" 1 per-lane mask tests, 2 compacted triples
 //                               (default: per-face point records)
 //   "mesh.exhaustive.grad.faces" faces per CTA of the point-record gradient (8)
 //   "mesh.exhaustive.grad.occupancy" 4: that kernel capped for 4 CTAs/SM (64
 //                               registers) instead of 3
+//   "mesh.exhaustive.grad.lchunk" lasers per CTA of the point-record gradient
 //   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
 //   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk
 //   "mesh.visibility.queue"     1: queued BVH searches (visibility_queue_kernel)
