@@ -256,7 +256,9 @@ def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt, keys
 _GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.mode": 2},
                   {"mesh.exhaustive.grad.occupancy": 4}, {"mesh.exhaustive.grad.faces": 1},
                   {"mesh.exhaustive.grad.faces": 5}, {"mesh.exhaustive.grad.faces": 32},
-                  {"mesh.exhaustive.grad.lchunk": 5}, {"mesh.exhaustive.grad.lchunk": 8}]
+                  {"mesh.exhaustive.grad.lchunk": 5}, {"mesh.exhaustive.grad.lchunk": 8},
+                  {"mesh.exhaustive.grad.sslice": 7},
+                  {"mesh.exhaustive.grad.sslice": 32, "mesh.exhaustive.grad.lchunk": 5}]
 
 
 @pytest.mark.parametrize("keys", _GRAD_VARIANTS, ids=lambda k: ",".join(

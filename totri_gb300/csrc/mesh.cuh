@@ -766,8 +766,8 @@ __device__ __forceinline__ bool target_visible_pp(const Scene& sc, int b, int n,
 // include every occluder the rays' own BVH walks would test, and the exact
 // triangle test decides.
 struct Shaft {
-  float plo[3], nplrl[3], rl[3];  // lower face: Plo + s (Clo - Plo) <= box hi
-  float phi[3], nphrh[3], rh[3];  // upper face: Phi + s (Chi - Phi) >= box lo
+  float plo[3], rl[3];  // lower face: Plo + s (Clo - Plo) <= box hi
+  float phi[3], rh[3];  // upper face: Phi + s (Chi - Phi) >= box lo
   bool lneg[3], hneg[3];
 };
 
@@ -780,8 +780,6 @@ __device__ __forceinline__ Shaft make_shaft(const float plo[3], const float phi[
     h.phi[a] = phi[a];
     h.rl[a] = 1.f / dl;
     h.rh[a] = 1.f / dh;
-    h.nplrl[a] = -(plo[a] * h.rl[a]);
-    h.nphrh[a] = -(phi[a] * h.rh[a]);
     h.lneg[a] = dl < 0.f;
     h.hneg[a] = dh < 0.f;
   }
@@ -789,15 +787,20 @@ __device__ __forceinline__ Shaft make_shaft(const float plo[3], const float phi[
 }
 
 // Box [lo, hi] against the hull; a NaN bound (a zero extent meeting a box
-// face exactly) drops its constraint, which can only admit a box.
+// face exactly) drops its constraint, which can only admit a box. Each bound
+// is the difference of coordinates, then scaled: its error is an ulp of the
+// coordinates over |dl|, inside the pad / |dl| that the grown boxes leave in
+// s. (Scaling first, hi / dl - Plo / dl, cancels two huge terms when an axis
+// of the hull is short, e.g. a target point beside the wall patch's box edge,
+// and rejected boxes holding occluders.)
 __device__ __forceinline__ bool shaft_box(const Shaft& h, float lx, float ly, float lz, float hx,
                                           float hy, float hz) {
   const float lo[3] = {lx, ly, lz}, hi[3] = {hx, hy, hz};
   float smin = 0.f, smax = 1.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float u = fmaf(hi[a], h.rl[a], h.nplrl[a]);  // (hi - Plo) / dl
-    const float w = fmaf(lo[a], h.rh[a], h.nphrh[a]);  // (lo - Phi) / dh
+    const float u = (hi[a] - h.plo[a]) * h.rl[a];  // (hi - Plo) / dl
+    const float w = (lo[a] - h.phi[a]) * h.rh[a];  // (lo - Phi) / dh
     if (h.lneg[a]) smin = fmaxf(smin, u);
     else smax = fminf(smax, u);
     if (h.hneg[a]) smax = fminf(smax, w);

@@ -189,10 +189,11 @@ __global__ void __launch_bounds__(256, kOcc) visibility_patch_kernel(Scene sc, V
         if (okp)
           need = query_prefix(sc, b, n, tg, o, seed, seed_mode, seed_steps, dir, tmax, tf, vis);
         if (__any_sync(0xffffffffu, need)) {
-          // every ray ends at the target's hit point, its centroid up to the
-          // rounding of t (far below pad)
-          const float clo[3] = {tg.c.x - pad, tg.c.y - pad, tg.c.z - pad};
-          const float chi[3] = {tg.c.x + pad, tg.c.y + pad, tg.c.z + pad};
+          // every ray ends at its accepted hit on the target, which tri_hit
+          // keeps inside the target's hit box (not near the centroid: for a
+          // grazing target t is ill-conditioned along the ray)
+          const float clo[3] = {tg.a2.y - pad, tg.a2.z - pad, tg.a2.w - pad};
+          const float chi[3] = {tg.a3.x + pad, tg.a3.y + pad, tg.a3.z + pad};
           const Shaft h = make_shaft(plo, phi, clo, chi);
           int* wb = shaft_buf + warp * (2 * kShaftFrontier + kShaftCand);
           int* cand = wb + 2 * kShaftFrontier;

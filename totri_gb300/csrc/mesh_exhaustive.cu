@@ -578,7 +578,7 @@ __device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* tota
 template <int kOcc>
 __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
     Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
-    int T, float bw, float bo, GradOut out, int faces_per_cta, int lchunk) {
+    int T, float bw, float bo, GradOut out, int faces_per_cta, int lchunk, int sslice) {
   extern __shared__ float recs[];        // scan-point then laser-point records, SoA
   float* srec = recs;
   float* lrec = recs + kRec * kFaceSlice;
@@ -588,8 +588,8 @@ __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
   const int b = blockIdx.y;
   const int n = sc.meta[b].n;
   const int nlc = (L + lchunk - 1) / lchunk;
-  const int s0 = (blockIdx.z / nlc) * kFaceSlice;
-  const int ns_all = min(kFaceSlice, S - s0);
+  const int s0 = (blockIdx.z / nlc) * sslice;
+  const int ns_all = min(sslice, S - s0);
   const int la = (blockIdx.z % nlc) * lchunk, lb = min(L, la + lchunk);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float* tgb = tgrad + (size_t)b * T * S * L;
@@ -890,32 +890,38 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   if (mode != 1 && mode != 2) {
     // "mesh.exhaustive.grad.faces": faces per CTA (default 8);
     // "mesh.exhaustive.grad.occupancy" = 4: registers capped for 4 CTAs per SM
-    // (64, with spills) instead of 3 (80). Lasers are split into chunks of
-    // `lchunk` per CTA, faces varying fastest over the grid, so the CTAs that
-    // run together read the transient_grad rows of one (scan slice, laser
-    // chunk): at 64x64 x 16x16 points that footprint no longer fits L2 with
-    // all 256 lasers per CTA (0.37 against 0.23 ms per thousand pairs at
-    // 64x64 x 8x8). "mesh.exhaustive.grad.lchunk" overrides.
+    // (64, with spills) instead of 3 (80). Each CTA takes `sslice` scan points
+    // and `lchunk` lasers, faces varying fastest over the grid, so the CTAs
+    // that run together read the transient_grad rows of one (scan slice, laser
+    // chunk). When a bin row of transient_grad (S L floats) reaches 2 MB the
+    // per-pair cost grows (one 20k-face mesh, 2,048 bins: 0.23 ms per thousand
+    // pairs at 64x64 x 8x8 points, 0.36 at 64x64 x 16x16), and 128 scan points
+    // by 32 lasers per CTA recover part of it (378 -> 331 ms at 64x64 x 16x16;
+    // at 32x32 x 16x16 whole 256 x 256 tiles stay faster, 54.8 against
+    // 58.5 ms). "mesh.exhaustive.grad.sslice" / ".lchunk" override.
     const int fpc = tune::get("mesh.exhaustive.grad.faces") > 0
                         ? (int)tune::get("mesh.exhaustive.grad.faces")
                         : kFacesPerCta;
+    const bool wide_rows = (int64_t)S * L >= (int64_t)1 << 19;
     int lchunk = tune::get("mesh.exhaustive.grad.lchunk");
-    if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = kFaceSlice;
+    if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = wide_rows ? 32 : kFaceSlice;
+    int sslice = tune::get("mesh.exhaustive.grad.sslice");
+    if (sslice <= 0 || sslice > kFaceSlice) sslice = wide_rows ? 128 : kFaceSlice;
     const bool occ4 = tune::get("mesh.exhaustive.grad.occupancy") == 4;
     const void* fn = occ4 ? reinterpret_cast<const void*>(exh_grad_face_kernel<4>)
                           : reinterpret_cast<const void*>(exh_grad_face_kernel<3>);
     const size_t smem = sizeof(float) * 2 * kRec * kFaceSlice;
     TOTRI_CUDA(tune::ensure_dynamic_smem(fn, smem));
     const dim3 grid((unsigned)ceil_div(sc.F, fpc), (unsigned)sc.B,
-                    (unsigned)(ceil_div(S, kFaceSlice) * ceil_div(L, lchunk)));
+                    (unsigned)(ceil_div(S, sslice) * ceil_div(L, lchunk)));
     if (occ4)
       TOTRI_KERNEL("mesh exhaustive grad", stream,
                    exh_grad_face_kernel<4><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk));
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk, sslice));
     else
       TOTRI_KERNEL("mesh exhaustive grad", stream,
                    exh_grad_face_kernel<3><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk));
+                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk, sslice));
     return TOTRI_OK;
   }
   if (mode == 1) {

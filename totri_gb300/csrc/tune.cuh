@@ -15,9 +15,11 @@
 //   "mesh.exhaustive.grad.faces" faces per CTA of the point-record gradient (8)
 //   "mesh.exhaustive.grad.occupancy" 4: that kernel capped for 4 CTAs/SM (64
 //                               registers) instead of 3
-//   "mesh.exhaustive.grad.lchunk" lasers per CTA of the point-record gradient
+//   "mesh.exhaustive.grad.lchunk", ".sslice" lasers / scan points per CTA of the
+//                               point-record gradient (at most 256 each)
 //   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
-//   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk
+//   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk, 7 one hull
+//                               per target (at its launcher)
 //   "mesh.visibility.queue"     1: queued BVH searches (visibility_queue_kernel)
 //   "mesh.visibility.wide"      2: binary BVH search after the surface-walk prefix
 //                               (the default is the 4-wide search)
