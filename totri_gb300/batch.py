@@ -52,6 +52,17 @@ class _Wave:
         self.member_ids = torch.tensor(members, dtype=torch.int64, device=dev)
 
 
+def chunked_dot(a, b, chunk=1 << 30):
+    """<a, b> over all elements as a sum of dot products of at most `chunk`
+    elements each: cuBLAS takes 32-bit vector lengths, and one mesh's
+    exhaustive transient (2,048 bins x 64x64 x 16x16 points) holds 2^31."""
+    a, b = a.reshape(-1), b.reshape(-1)
+    parts = [torch.dot(a[i:i + chunk], b[i:i + chunk]) for i in range(0, a.numel(), chunk)]
+    if not parts:
+        return torch.zeros((), dtype=a.dtype, device=a.device)
+    return parts[0] if len(parts) == 1 else torch.stack(parts).sum()
+
+
 class BatchedMeshRenderer:
     """Forward and vertex/albedo gradient of many meshes against one wall setup.
 
@@ -212,8 +223,7 @@ class BatchedMeshRenderer:
                     ctypes.c_void_p(tg[pos].data_ptr()), tg[pos].numel(),
                     self.normal_seed + i, _lib.stream_of(self.device)))
             # one dot product per mesh (no transient-sized temporary)
-            dots = torch.stack([torch.dot(tr[p].reshape(-1), tg[p].reshape(-1))
-                                for p in range(n)])
+            dots = torch.stack([chunked_dot(tr[p], tg[p]) for p in range(n)])
             self.loss.index_copy_(0, w.member_ids, dots)
         elif callable(self.grad):
             self.grad(list(w.members), tr, self.transient_grad[:n])

@@ -527,6 +527,75 @@ __global__ void __launch_bounds__(256) confocal_adjoint_cells_kernel(Geo g, Poin
   }
 }
 
+constexpr int kAdjUnroll = 4;  // bins per step of the lanes-over-columns adjoint
+
+// The bins [t0, t1] of one point for the lanes' columns, kAdjUnroll at a time:
+// the fast path without branches (a sample that is not taken adds zero to
+// cell 0), then the few samples that sit within the rounding margin of a cell
+// boundary through the exact chain. Without kCheck (the bins with
+// non-negative centres, walked last) the step may run up to kAdjUnroll - 1
+// bins past t1: those are real bins (walked with their values, and rejected
+// unless they hold a sample) up to T - 1, and table padding (tc^2 = -inf)
+// beyond it; with kCheck (the negative centres, whose later bins belong to
+// the other walk) bins past t1 are skipped. z_hat = (depth + (wz - oz)) scale
+// - 0.5: the rounding of either association is inside sample_filtered's
+// margin.
+template <bool kCheck>
+__device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict__ tab,
+                                         const float* __restrict__ row, float* col, int t0,
+                                         int t1, int lane, float ddx, float ddy, float wz,
+                                         float wzo, float pm, float wx, float wy, float x,
+                                         float y) {
+  const int tend = kCheck ? t1 : g.T - 1;  // last bin whose value is read
+  float wval = 0.f;                        // bin t0 + 32 k + lane
+  for (int t = t0; t <= t1; t += kAdjUnroll) {
+    const int wo = (t - t0) & 31;
+    if (wo == 0) wval = t + lane <= tend ? __ldg(row + t + lane) : 0.f;
+    int zi[kAdjUnroll];
+    float w0[kAdjUnroll], w1[kAdjUnroll];
+    bool slow[kAdjUnroll];
+    bool any_slow = false;
+#pragma unroll
+    for (int q = 0; q < kAdjUnroll; ++q) {
+      const float val = __shfl_sync(0xffffffffu, wval, wo + q);
+      const float2 tb = (!kCheck || t + q <= t1) ? tab[t + q] : make_float2(-INFINITY, 0.f);
+      const float d2 = xsub(xsub(tb.x, ddx), ddy);
+      const bool valid = d2 > 0.f;
+      const float depth = d2 * rsqrtf(d2);  // NaN when d2 <= 0: never taken
+      const float zh = fmaf(depth + wzo, g.scale, -0.5f);
+      const float fl = floorf(zh);
+      const float fr = zh - fl;
+      const bool fast = !g.exact && fabsf(fr - 0.5f) < 0.5f - pm;
+      const int z = __float2int_rz(fl);
+      const bool ok = valid && fast && (unsigned)z < (unsigned)(g.Z - 1);
+      const float v = val * ((d2 * d2) * tb.y);
+      zi[q] = ok ? z : 0;
+      w0[q] = ok ? (1.f - fr) * v : 0.f;
+      w1[q] = ok ? fr * v : 0.f;
+      slow[q] = valid && !fast;
+      any_slow |= slow[q];
+    }
+    if (__any_sync(0xffffffffu, any_slow)) {
+#pragma unroll
+      for (int q = 0; q < kAdjUnroll; ++q) {
+        if (!slow[q]) continue;
+        const Sample sm = sample(g, wx, wy, wz, t + q, x, y);
+        if (sm.ok) {
+          const float vv = __ldg(row + t + q) * sm.f2;
+          zi[q] = sm.zi;
+          w0[q] = (1.f - sm.alpha) * vv;
+          w1[q] = sm.alpha * vv;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kAdjUnroll; ++q) {
+      col[zi[q] * 32] += w0[q];
+      col[zi[q] * 32 + 32] += w1[q];
+    }
+  }
+}
+
 // Exact adjoint of the forward with the lanes of a warp over 32 neighbouring
 // voxel columns (an 8 x 4 tile: y fastest) and all lanes on one point and one
 // bin at a time. The point's transient row is then read once per warp (32 bins
@@ -545,8 +614,6 @@ __global__ void __launch_bounds__(256) confocal_adjoint_cells_kernel(Geo g, Poin
 // in its own span, and a sample outside it is decided (and rejected) like any
 // other, so each (column, point, bin) is counted once. Decisions are the exact
 // chain's (sample_filtered's margin, taken over the largest |tc| of the union).
-constexpr int kAdjUnroll = 4;  // bins per step of the lanes-over-columns adjoint
-
 __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
     Geo g, Points mp, int N, int points_per_group, const float* __restrict__ tr,
     float* __restrict__ vol, int accumulate) {
@@ -558,7 +625,11 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
   const int yi = ty + (lane & 7), xi = tx + (lane >> 3);
   const bool live = xi < g.X && yi < g.Y;
   for (int j = threadIdx.x; j < nw * g.Z * 32; j += blockDim.x) acc[j] = 0.f;
-  for (int t = threadIdx.x; t < g.T; t += blockDim.x) {
+  for (int t = threadIdx.x; t < g.T + kAdjUnroll; t += blockDim.x) {
+    if (t >= g.T) {  // padding: no sample
+      tab[t] = make_float2(-INFINITY, 0.f);
+      continue;
+    }
     const float tc = xadd(xmul((float)t, g.bw), g.bo);
     const float tc2 = xmul(tc, tc);
     const float i2 = __fdividef(1.f, tc2);
@@ -607,61 +678,10 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
       const float pm = 8.f * u * g.scale * (dmax + fabsf(wz) + zmax + fabsf(g.oz)) +
                        4.f * u * zhmax + 1e-7f;
       const float* row = tr + (size_t)(base + j) * g.T;
-      for (int r = 0; r < 2; ++r) {
-        const int t0 = r ? n0 : p0, t1 = r ? n1 : p1;
-        float wval = 0.f;  // bin t0 + 32 k + lane
-        for (int t = t0; t <= t1; t += kAdjUnroll) {
-          const int wo = (t - t0) & 31;
-          if (wo == 0) wval = t + lane <= t1 ? __ldg(row + t + lane) : 0.f;
-          // kAdjUnroll independent samples: the fast path without branches (a
-          // sample that is not taken adds zero to cell 0), then the few that
-          // sit within the rounding margin of a cell boundary through the
-          // exact chain
-          int zi[kAdjUnroll];
-          float w0[kAdjUnroll], w1[kAdjUnroll];
-          bool slow[kAdjUnroll];
-          bool any_slow = false;
-#pragma unroll
-          for (int q = 0; q < kAdjUnroll; ++q) {
-            const float val = __shfl_sync(0xffffffffu, wval, wo + q);
-            const float2 tb = t + q <= t1 ? tab[t + q] : make_float2(-INFINITY, 0.f);
-            const float d2 = xsub(xsub(tb.x, ddx), ddy);
-            const bool valid = d2 > 0.f;
-            const float depth = d2 * rsqrtf(fmaxf(d2, 1e-30f));
-            const float zh = fmaf((wz + depth) - g.oz, g.scale, -0.5f);
-            const float fl = floorf(zh);
-            const float fr = zh - fl;
-            const bool fast = !g.exact && fabsf(fr - 0.5f) < 0.5f - pm;
-            const int z = __float2int_rz(fl);
-            const bool ok = valid && fast && (unsigned)z < (unsigned)(g.Z - 1);
-            const float v = val * ((d2 * d2) * tb.y);
-            zi[q] = ok ? z : 0;
-            w0[q] = ok ? (1.f - fr) * v : 0.f;
-            w1[q] = ok ? fr * v : 0.f;
-            slow[q] = valid && !fast;
-            any_slow |= slow[q];
-          }
-          if (__any_sync(0xffffffffu, any_slow)) {
-#pragma unroll
-            for (int q = 0; q < kAdjUnroll; ++q) {
-              if (!slow[q]) continue;
-              const Sample sm = sample(g, wx, wy, wz, t + q, x, y);
-              if (sm.ok) {
-                const float val = __ldg(row + t + q);
-                const float vv = val * sm.f2;
-                zi[q] = sm.zi;
-                w0[q] = (1.f - sm.alpha) * vv;
-                w1[q] = sm.alpha * vv;
-              }
-            }
-          }
-#pragma unroll
-          for (int q = 0; q < kAdjUnroll; ++q) {
-            col[zi[q] * 32] += w0[q];
-            col[zi[q] * 32 + 32] += w1[q];
-          }
-        }
-      }
+      const float wzo = wz - g.oz;
+      adj_walk<false>(g, tab, row, col, p0, p1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y);
+      if (n0 <= n1)  // warp-uniform: negative bin centres (a negative bin offset)
+        adj_walk<true>(g, tab, row, col, n0, n1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y);
     }
   }
   __syncthreads();
@@ -845,7 +865,7 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
   // lanes over columns: warps per CTA such that two CTAs' copies of 32
   // columns and the bin table fit an SM's shared memory
   // ("volume.adjoint.warps" overrides); bins beyond 4,096 take the atomic kernel
-  const size_t table = sizeof(float2) * (size_t)T;
+  const size_t table = sizeof(float2) * ((size_t)T + volume::kAdjUnroll);
   const size_t per_warp = (size_t)Z * 32 * sizeof(float);
   int warps = T <= 4096 && table < 113 * 1024 ? (int)((113 * 1024 - table) / per_warp) : 0;
   if (tune::get("volume.adjoint.warps") > 0) warps = tune::get("volume.adjoint.warps");
