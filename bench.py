@@ -351,7 +351,7 @@ def batched_metrics(device, count=32, steps=2, seed=1234):
     which bounds what any batching of these calls can gain. Unit: (face,
     detector point, laser point) triples per second."""
     from totri_gb300 import _lib, scenes
-    from totri_gb300.batch import BatchedMeshRenderer
+    from totri_gb300.batch import BatchedMeshRenderer, chunked_dot
     from totri_gb300.totri_cpp import render as R
     s = scenes.batched_exhaustive(count=count)
     meshes = [tuple(t.to(device) for t in m) for m in s["meshes"]]
@@ -407,7 +407,7 @@ def batched_metrics(device, count=32, steps=2, seed=1234):
             tg = torch.empty_like(out)
             _lib.check(lib.totri_fill_normal(ctypes.c_void_p(tg.data_ptr()), tg.numel(),
                                              seed + i, _lib.stream_of(device)))
-            torch.dot(out.reshape(-1), tg.reshape(-1))
+            chunked_dot(out, tg)  # the loss, as the batched normal head forms it
             del out
             vg, mg = torch.empty_like(v), torch.empty_like(m)
             R.mesh_exhaustive_grad_verts(v, f, m, sp[None], lp[None], so, so, tg, vg, mg,
