@@ -162,6 +162,23 @@ __device__ __forceinline__ fv3 cross(fv3 a, fv3 b) {
   return fv3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 
+// Two floats in one 64-bit register pair, for the paired FP32 FMA of sm_100
+// and later (fma.rn.f32x2): each half is one correctly rounded fma, the same
+// value fmaf gives.
+__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
 // Monotone float <-> int mapping for atomicMin/atomicMax on floats.
 __device__ __forceinline__ int ford(float f) {
   const int i = __float_as_int(f);

@@ -231,24 +231,6 @@ __device__ __forceinline__ float safe_inv(float d) {
   return fabsf(d) < 1e-20f ? copysignf(1e20f, d) : 1.f / d;
 }
 
-// Two floats in one 64-bit register pair, for the paired FP32 FMA of sm_100
-// and later (fma.rn.f32x2): each half is one correctly rounded fma, the same
-// value fmaf gives.
-__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
-                                                    unsigned long long c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-
 // A ray's slab constants for node_slabs: 1/d and -o/d as (x, y) and (z, z)
 // pairs.
 struct RaySlab {
