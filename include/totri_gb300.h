@@ -158,6 +158,27 @@ int totri_mesh_confocal_grad_verts_reuse(const totri_array_t* verts,
                                          void* workspace, size_t workspace_bytes,
                                          void* stream);
 
+/* The confocal forward and gradient with every (scan point, face) pair
+ * counted as visible: the unoccluded three-bounce render (arguments, layouts
+ * and workspace as for totri_mesh_confocal_forward / _grad_verts; a
+ * totri_mesh_confocal_grad_verts_reuse call after the unoccluded forward
+ * reuses its all-visible masks). No reference counterpart: the reference
+ * always tests visibility (mesh_confocal_forward_optix.cu:50-66). */
+int totri_mesh_confocal_forward_unoccluded(const totri_array_t* verts,
+                                           const totri_array_t* faces,
+                                           const totri_array_t* material,
+                                           const totri_array_t* scan_points,
+                                           const totri_array_t* scan_origin,
+                                           const totri_array_t* transient, float bin_width,
+                                           float bin_offset, int model, void* workspace,
+                                           size_t workspace_bytes, void* stream);
+int totri_mesh_confocal_grad_verts_unoccluded(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* scan_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bin_width, float bin_offset, int model,
+    void* workspace, size_t workspace_bytes, void* stream);
+
 /* Replaces totri_cpp.render.mesh_exhaustive_forward
  * (src/render/mesh.h:31-42, src/render/mesh.cpp:38-52).
  * laser_points [B,L,3], laser_origin [B,L,3] or [B,0,3]; transient [B,T,S,L]. */

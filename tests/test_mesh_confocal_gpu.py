@@ -366,3 +366,40 @@ def test_seeded_visibility_without_or_with_odd_adjacency(cuda_lib, kernel):
             got = _with_keys(kernel, lambda: _with_seed(case, lambda: R.mesh_visibility(
                 verts.cuda(), faces.cuda(), pts.cuda())))
             assert np.array_equal(unpack_mask(got[0].cpu().numpy(), F), ref), (kernel, case)
+
+
+def test_unoccluded_render_and_gradient_match_oracle_without_visibility(cuda_lib):
+    """The unoccluded three-bounce render of the config-0 scene (level-2
+    icosphere, 32x32 scan, 512 bins): every (scan point, face) pair counts, as
+    the FP64 oracle with an all-ones mask computes it; through the C ABI and
+    through MeshRenderConfocal.apply(..., visibility=False) forward and
+    backward (whose gradient reuses the forward's all-visible masks)."""
+    s = scenes.confocal_small()
+    d, n = _dev(s), np_scene(s)
+    bd = s["bin_def"]
+    S, F = n["scan_points"].shape[0], n["faces"].shape[0]
+    ones = np.ones((S, F), np.uint8)
+    ref = _oracle_forward(n, ones, bd)
+    vis = oracle.mesh_visibility(n["verts"], n["faces"], n["scan_points"])
+    assert np.abs(ref).sum() > 1.2 * np.abs(_oracle_forward(n, vis, bd)).sum()  # occlusion matters
+    empty = torch.empty_like(d["scan_points"][:, :0])
+    out = torch.full((1, bd.num, S), 7.0, device="cuda")
+    R.mesh_confocal_forward_unoccluded(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                                       empty, out, bd.width, bd.offset, 0)
+    assert rel_l2(out[0].double().cpu().numpy(), ref) < FWD_TOL
+    tg = np.random.default_rng(4).standard_normal(ref.shape)
+    rv, rm = oracle.mesh_confocal_grad(n["verts"], n["faces"], n["colors"], n["scan_points"],
+                                       None, ones, bd.num, bd.width, bd.offset, tg)
+    vg, mg = torch.empty_like(d["verts"]), torch.empty_like(d["colors"])
+    R.mesh_confocal_grad_verts_unoccluded(d["verts"], d["faces"], d["colors"], d["scan_points"],
+                                          empty, torch.tensor(tg, dtype=torch.float32)[None].cuda(),
+                                          vg, mg, bd.width, bd.offset, 0)
+    assert rel_l2(vg[0].double().cpu().numpy(), rv) < GRAD_TOL
+    assert rel_l2(mg[0].double().cpu().numpy(), rm) < GRAD_TOL
+    verts = d["verts"].clone().requires_grad_(True)
+    colors = d["colors"].clone().requires_grad_(True)
+    tr = MeshRenderConfocal.apply(verts, d["faces"], d["scan_points"], bd, colors, None, False)
+    assert rel_l2(tr[0].detach().double().cpu().numpy(), ref) < FWD_TOL
+    (tr * torch.tensor(tg, dtype=torch.float32)[None].cuda()).sum().backward()
+    assert rel_l2(verts.grad[0].double().cpu().numpy(), rv) < GRAD_TOL
+    assert rel_l2(colors.grad[0].double().cpu().numpy(), rm) < GRAD_TOL

@@ -88,6 +88,9 @@ _SIGNATURES = {
     "totri_mesh_confocal_forward": [_ArrP] * 6 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_confocal_grad_verts": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_confocal_grad_verts_reuse": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz, _vp],
+    "totri_mesh_confocal_forward_unoccluded": [_ArrP] * 6 + [_flt, _flt, _int, _vp, _sz, _vp],
+    "totri_mesh_confocal_grad_verts_unoccluded": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz,
+                                                               _vp],
     "totri_mesh_exhaustive_forward": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_exhaustive_grad_verts": [_ArrP] * 10 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_exhaustive_grad_verts_reuse": [_ArrP] * 10 + [_flt, _flt, _int, _vp, _sz, _vp],

@@ -147,13 +147,20 @@ int check_masks(const void* masks, size_t bytes, int64_t B, int64_t F, int64_t P
   return TOTRI_OK;
 }
 
+// Every (point, face) pair visible: the masks of the unoccluded renders.
+int all_visible(const mesh::Scene& sc, int64_t P, cudaStream_t stream) {
+  TOTRI_CUDA(cudaMemsetAsync(sc.mask, 0xff, sizeof(uint32_t) * (size_t)sc.B * P * sc.nch,
+                             stream));
+  return TOTRI_OK;
+}
+
 int confocal_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
                        const totri_array_t* material, const totri_array_t* scan_points,
                        const totri_array_t* scan_origin, const totri_array_t* transient_grad,
                        const totri_array_t* verts_grad, const totri_array_t* material_grad,
                        float bin_width, float bin_offset, void* ws, size_t ws_bytes,
                        void* stream_, bool reuse, void* masks = nullptr,
-                       size_t masks_bytes = 0) {
+                       size_t masks_bytes = 0, bool occluded = true) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   MeshArgs a;
   TOTRI_TRY(check_mesh(verts, faces, material, a));
@@ -182,7 +189,10 @@ int confocal_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
   }
   if (!reuse && !masks) {
     TOTRI_TRY(mesh::build_scene(sc, a.in, stream));
-    TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)S, 0, false, stream));
+    if (occluded)
+      TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)S, 0, false, stream));
+    else
+      TOTRI_TRY(all_visible(sc, S, stream));
   }
   return mesh::launch_confocal_grad(sc, view3f(scan_points), view3f(scan_origin), has_origin,
                                     static_cast<const float*>(transient_grad->data), (int)T,
@@ -268,14 +278,13 @@ size_t totri_mesh_workspace(int64_t batch, int64_t num_verts, int64_t num_faces,
   return mesh::layout(batch, num_faces, num_points).total;
 }
 
-int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t* faces,
-                                const totri_array_t* material,
-                                const totri_array_t* scan_points,
-                                const totri_array_t* scan_origin,
-                                const totri_array_t* transient, float bin_width,
-                                float bin_offset, int model, void* ws, size_t ws_bytes,
-                                void* stream_) {
-  (void)model;
+static int confocal_forward_impl(const totri_array_t* verts, const totri_array_t* faces,
+                                 const totri_array_t* material,
+                                 const totri_array_t* scan_points,
+                                 const totri_array_t* scan_origin,
+                                 const totri_array_t* transient, float bin_width,
+                                 float bin_offset, void* ws, size_t ws_bytes, void* stream_,
+                                 bool occluded) {
   cudaStream_t stream = static_cast<cudaStream_t>(stream_);
   MeshArgs a;
   TOTRI_TRY(check_mesh(verts, faces, material, a));
@@ -299,10 +308,50 @@ int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t*
   TOTRI_TRY(check_workspace(ws, ws_bytes, L.total));
   const mesh::Scene sc = mesh::scene_from_workspace(ws, a.B, a.F, S);
   TOTRI_TRY(mesh::build_scene(sc, a.in, stream));
-  TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)S, 0, false, stream));
+  if (occluded)
+    TOTRI_TRY(mesh::launch_visibility(sc, view3f(scan_points), (int)S, 0, false, stream));
+  else
+    TOTRI_TRY(all_visible(sc, S, stream));
   return mesh::launch_confocal_splat(sc, view3f(scan_points), view3f(scan_origin), has_origin,
                                      static_cast<float*>(transient->data), (int)T, (int)S,
                                      bin_width, bin_offset, stream);
+}
+
+int totri_mesh_confocal_forward(const totri_array_t* verts, const totri_array_t* faces,
+                                const totri_array_t* material,
+                                const totri_array_t* scan_points,
+                                const totri_array_t* scan_origin,
+                                const totri_array_t* transient, float bin_width,
+                                float bin_offset, int model, void* ws, size_t ws_bytes,
+                                void* stream) {
+  (void)model;
+  return confocal_forward_impl(verts, faces, material, scan_points, scan_origin, transient,
+                               bin_width, bin_offset, ws, ws_bytes, stream, true);
+}
+
+int totri_mesh_confocal_forward_unoccluded(const totri_array_t* verts,
+                                           const totri_array_t* faces,
+                                           const totri_array_t* material,
+                                           const totri_array_t* scan_points,
+                                           const totri_array_t* scan_origin,
+                                           const totri_array_t* transient, float bin_width,
+                                           float bin_offset, int model, void* ws,
+                                           size_t ws_bytes, void* stream) {
+  (void)model;
+  return confocal_forward_impl(verts, faces, material, scan_points, scan_origin, transient,
+                               bin_width, bin_offset, ws, ws_bytes, stream, false);
+}
+
+int totri_mesh_confocal_grad_verts_unoccluded(
+    const totri_array_t* verts, const totri_array_t* faces, const totri_array_t* material,
+    const totri_array_t* scan_points, const totri_array_t* scan_origin,
+    const totri_array_t* transient_grad, const totri_array_t* verts_grad,
+    const totri_array_t* material_grad, float bin_width, float bin_offset, int model, void* ws,
+    size_t ws_bytes, void* stream) {
+  (void)model;
+  return confocal_grad_impl(verts, faces, material, scan_points, scan_origin, transient_grad,
+                            verts_grad, material_grad, bin_width, bin_offset, ws, ws_bytes,
+                            stream, false, nullptr, 0, false);
 }
 
 int totri_mesh_confocal_grad_verts(const totri_array_t* verts, const totri_array_t* faces,

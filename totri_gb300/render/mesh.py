@@ -40,6 +40,9 @@ class MeshRenderConfocal(torch.autograd.Function):
         colors (torch.Tensor, optional): Color of each vertex [B, V, 1].
         scan_origin (torch.Tensor, optional): Laser/detector position per scan point
             [B, S, 3], [B, 1, 3] or [B, 3].
+        visibility (bool, optional): False renders every (scan point, face) pair
+            as visible (the unoccluded render; an extension, default True as the
+            reference).
 
     Returns:
         torch.Tensor: Transient image [B, T, S]
@@ -49,7 +52,8 @@ class MeshRenderConfocal(torch.autograd.Function):
     def forward(ctx, verts: torch.Tensor, faces: typing.Optional[torch.Tensor],
                 scan_points: torch.Tensor, bin_def: BinDef,
                 colors: typing.Optional[torch.Tensor] = None,
-                scan_origin: typing.Optional[torch.Tensor] = None) -> torch.Tensor:
+                scan_origin: typing.Optional[torch.Tensor] = None,
+                visibility: bool = True) -> torch.Tensor:
         _lib.require_cuda(verts, scan_points)
         faces = faces_of_verts(verts, faces)
         colors = colors_of_verts(colors, verts)
@@ -60,15 +64,16 @@ class MeshRenderConfocal(torch.autograd.Function):
         B, V, F, S = verts.shape[0], verts.shape[1], faces.shape[1], scan_points.shape[1]
         transient = torch.empty((B, bin_def.num, S), device=verts.device, dtype=torch.float32)
         ws = mesh_workspace(B, V, F, S, verts.device)
-        _run("totri_mesh_confocal_forward",
+        _run("totri_mesh_confocal_forward" if visibility
+             else "totri_mesh_confocal_forward_unoccluded",
              (verts, faces, colors, scan_points, scan_origin, transient), bin_def, ws,
              verts.device)
-        ctx.workspace = ws
+        ctx.workspace = ws  # the backward reuses its masks (all visible when unoccluded)
         return transient
 
     @staticmethod
     def backward(ctx, transient_grad: torch.Tensor):
-        grad = [None] * 6
+        grad = [None] * 7
         if transient_grad is None:
             return tuple(grad)
         need = _needs(ctx)

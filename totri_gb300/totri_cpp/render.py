@@ -43,6 +43,31 @@ def mesh_confocal_grad_verts(verts, faces, material, scan_points, scan_origin, t
                bin_width, bin_offset, model, scan_points.shape[1])
 
 
+def mesh_confocal_forward_unoccluded(verts, faces, material, scan_points, scan_origin,
+                                     transient, bin_width, bin_offset, model):
+    """mesh_confocal_forward with every (scan point, face) pair visible: the
+    unoccluded three-bounce render (an extension; the reference always tests
+    visibility)."""
+    _lib.require_cuda(verts, faces, material, scan_points, scan_origin, transient)
+    out = dense_out(transient)
+    _mesh_call("totri_mesh_confocal_forward_unoccluded",
+               (verts, faces, material, scan_points, scan_origin, out), bin_width, bin_offset,
+               model, scan_points.shape[1])
+    finish_out(transient, out)
+
+
+def mesh_confocal_grad_verts_unoccluded(verts, faces, material, scan_points, scan_origin,
+                                        transient_grad, verts_grad, material_grad, bin_width,
+                                        bin_offset, model):
+    """mesh_confocal_grad_verts of the unoccluded render."""
+    _lib.require_cuda(verts, faces, material, scan_points, scan_origin, transient_grad,
+                      verts_grad, material_grad)
+    _mesh_call("totri_mesh_confocal_grad_verts_unoccluded",
+               (verts, faces, material, scan_points, scan_origin,
+                transient_grad.contiguous(), verts_grad, material_grad),
+               bin_width, bin_offset, model, scan_points.shape[1])
+
+
 def mesh_exhaustive_forward(verts, faces, material, scan_points, laser_points, scan_origin,
                             laser_origin, transient, bin_width, bin_offset, model):
     """transient [B,T,S,L] <- exhaustive render (reference src/render/mesh.cpp:38-52)."""
