@@ -165,6 +165,12 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
 
 constexpr int kChunk = 512;  // voxels of a gradient brick (8 x 8 x 8)
 
+// Floats per staged voxel of the gradient brick, rounded up to an odd count:
+// lane j reads voxel j, so an even record (8 floats for one attribute) put
+// 8 lanes on each of 4 banks (the gradient spent 9.7 short-scoreboard stalls
+// per issue on it), an odd one spreads a warp's reads over all 32 banks.
+__host__ __device__ constexpr int grad_stride(int A) { return (4 + 2 * (1 + A)) | 1; }
+
 // Gradient (rbf2volume_cuda.cu:124-201): a CTA per brick of 8 x 8 x 8 voxels,
 // whose coordinates, volume and volume_grad channels are staged in shared
 // memory. Gaussians come in tiles of 256, culled against the brick's box as
@@ -176,11 +182,12 @@ __global__ void __launch_bounds__(256) grad_kernel(Grid g, int b, Rbf r, int N, 
                                                    const float* __restrict__ vgrad,
                                                    float* __restrict__ rgrad, int64_t gsb,
                                                    int64_t gsn, int64_t gsc) {
-  extern __shared__ float sm[];  // [kChunk][4 + 2 * (1 + A)] : x y z valid | vol[1+A] | grad[1+A]
+  // [kChunk][grad_stride(A)]: x y z valid | vol[1+A] | grad[1+A] (| pad)
+  extern __shared__ float sm[];
   __shared__ int list[kTile];
   __shared__ int counts[8];
   const int A = C - 4;
-  const int stride = 4 + 2 * (1 + A);
+  const int stride = grad_stride(A);
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 8;
@@ -354,7 +361,7 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* r, const totri_array_t* 
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   if (nv == 0 || N == 0 || B == 0) return TOTRI_OK;
   const int A = C - 4;
-  const size_t smem = sizeof(float) * rbf::kChunk * (4 + 2 * (1 + A));
+  const size_t smem = sizeof(float) * rbf::kChunk * rbf::grad_stride(A);
   TOTRI_CUDA(tune::ensure_dynamic_smem(
       reinterpret_cast<const void*>(rbf::grad_kernel), smem));
   const int cull = tune::get("rbf.cull") != 1;
