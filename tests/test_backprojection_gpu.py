@@ -122,6 +122,15 @@ def test_velten_bins_exact(cuda_lib, offset, origin):
                                              torch.from_numpy(sp)[None].cuda(), so_t, vol, st,
                                              en, bw, offset)
     assert np.array_equal(vol[0].double().cpu().numpy(), ref)
+    from totri_gb300 import autotune
+    for grp in (1, 2):  # one bin window per tile, group windows
+        autotune.set_tile("backprojection.velten.groups", grp)
+        v2 = torch.empty_like(vol)
+        K.backprojection_confocal_velten_forward(torch.from_numpy(tr)[None].cuda(),
+                                                 torch.from_numpy(sp)[None].cuda(), so_t, v2, st,
+                                                 en, bw, offset)
+        autotune.set_tile("backprojection.velten.groups", 0)
+        assert np.array_equal(v2[0].double().cpu().numpy(), ref)
     # adjoint: a one-voxel volume of value 1 gives 1 exactly at its bin for every scan point
     one = np.zeros(res, np.float64)
     one[17, 5, 30] = 1.0
@@ -137,27 +146,40 @@ def test_velten_tiled_equals_untiled(cuda_lib):
     """The shared-memory tiled Velten kernel sums the same values in the same
     order as the one-voxel-per-thread kernel: identical volumes for 1, 2 and
     4 voxels per thread, with registers capped (the default) or not
-    ("backprojection.velten.occupancy" = 1), including grids that are not a multiple of the voxel
-    block and a scan whose bin windows overflow the staged rows."""
+    ("backprojection.velten.occupancy" = 1), and with one bin window per tile
+    or group windows ("backprojection.velten.groups" = 1, 2), including grids
+    that are not a multiple of the voxel block. The scans cover every staging
+    of a tile's bin rows (by a CPU model of the kernel's choice, for 4 voxels
+    per thread): with group windows, random points give per-point windows, the
+    64x64 wall grid with 2,048 bins into 96^3 voxels gives windows per 8 and
+    per 4 points, and 4,096 bins into 64^3 voxels gives per-point windows cut
+    at their first rows, the rest read from global memory; with one window
+    per tile, the fine-bin scans overflow it and read from global memory."""
     from totri_gb300 import autotune
     g = np.random.default_rng(5)
+    grid = scenes.wall_grid(64)[0].numpy()
     for res, S, T, bw in (((37, 29, 50), 300, 900, 0.004), ((16, 16, 16), 1000, 256, 0.05),
-                          ((21, 9, 11), 77, 400, 0.01)):
+                          ((21, 9, 11), 77, 400, 0.01), ((96, 96, 96), None, 2048, 0.0025),
+                          ((64, 64, 64), None, 4096, 0.00125)):
+        pts = grid if S is None else np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S),
+                                               np.zeros(S)], -1)
+        S = pts.shape[0]
         tr = torch.from_numpy(g.random((1, T, S), dtype=np.float32)).cuda()
-        sp = torch.from_numpy(np.stack([g.uniform(-1, 1, S), g.uniform(-1, 1, S),
-                                        np.zeros(S)], -1).astype(np.float32))[None].cuda()
+        sp = torch.from_numpy(pts.astype(np.float32))[None].cuda()
         out = []
-        for mode, vz, occ in ((1, 0, 0), (0, 1, 0), (0, 2, 0), (0, 4, 0), (0, 4, 1)):
+        variants = [(1, 0, 0, 0)] + [(0, vz, occ, grp) for vz, occ in ((1, 0), (2, 0), (4, 0), (4, 1))
+                                     for grp in (1, 2)]
+        for mode, vz, occ, grp in variants:
             autotune.set_tile("backprojection.velten.mode", mode)
             autotune.set_tile("backprojection.velten.vz", vz)
             autotune.set_tile("backprojection.velten.occupancy", occ)
+            autotune.set_tile("backprojection.velten.groups", grp)
             v = torch.empty((1,) + res, device="cuda")
             K.backprojection_confocal_velten_forward(tr, sp, torch.empty((1, 0, 3), device="cuda"),
                                                      v, (-0.5, -0.4, 0.5), (0.5, 0.45, 1.5), bw,
                                                      0.01)
             out.append(v)
-        autotune.set_tile("backprojection.velten.mode", 0)
-        autotune.set_tile("backprojection.velten.vz", 0)
-        autotune.set_tile("backprojection.velten.occupancy", 0)
+        for key in ("mode", "vz", "occupancy", "groups"):
+            autotune.set_tile("backprojection.velten." + key, 0)
         for o in out[1:]:
             assert torch.equal(out[0], o)

@@ -21,7 +21,9 @@ Cases (full size / --small):
                     forward and exact adjoint (--small: 32x32 columns of 128
                     cells x 64x64 points)
   velten            Velten confocal backprojection of a 1,024-bin 128x128 scan
-                    into 128^3 voxels (--small: 64^3 from 64x64)
+                    into 128^3 voxels (--small: 64^3 from 64x64; --volume-res,
+                    --scan-res and --bins set the sides and the bin count over
+                    the same 5.12 m)
   rbf               4,096 Gaussians into 128^3 voxels: forward and gradient
                     (--small: 1,024 Gaussians, 64^3)
 """
@@ -126,11 +128,13 @@ def case_volume(small):
         {"voxels": list(vol.shape), "points": int(mp.shape[1]), "bins": bd.num}
 
 
-def case_velten(small):
+def case_velten(small, volume_res=None, scan_res=None, bins=None):
     from .totri_cpp import reconstruct as K
-    res = 64 if small else 128
-    s = scenes.volume_scene(res=res, scan_res=res)
+    res = volume_res or (64 if small else 128)
+    s = scenes.volume_scene(res=res, scan_res=scan_res or res)
     vd, bd = s["volume_def"], s["bin_def"]
+    if bins:  # the same 5.12 m span in finer bins, as the serving mix's bin sets
+        bd = BinDef(5.12 / bins, 0.0, bins)
     sp = s["scan_points"].cuda()
     tr = torch.rand((1, bd.num, sp.shape[1]), device="cuda",
                     generator=torch.Generator(device="cuda").manual_seed(4))
@@ -167,9 +171,14 @@ def main(argv=None):
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--set", action="append", default=[], metavar="KEY=VALUE")
     p.add_argument("--scan-res", type=int, default=None,
-                   help="exhaustive: detector grid side (default 32, --small 16)")
+                   help="exhaustive: detector grid side (default 32, --small 16); "
+                   "velten: scan grid side (default the volume side)")
     p.add_argument("--laser-res", type=int, default=None,
                    help="exhaustive: laser grid side (default 16, --small 8)")
+    p.add_argument("--volume-res", type=int, default=None,
+                   help="velten: voxels per side (default 128, --small 64)")
+    p.add_argument("--bins", type=int, default=None,
+                   help="velten: bins over 5.12 m (default 1,024 of 0.005 m)")
     a = p.parse_args(argv)
     keys = {}
     for kv in a.set:
@@ -179,6 +188,8 @@ def main(argv=None):
     extra = {}
     if a.case == "exhaustive":
         extra = dict(scan_res=a.scan_res, laser_res=a.laser_res)
+    elif a.case == "velten":
+        extra = dict(volume_res=a.volume_res, scan_res=a.scan_res, bins=a.bins)
     calls, config = CASES[a.case](a.small, **extra)
     ms = _timed(calls, a.reps)
     print(json.dumps({"case": a.case, "small": a.small, "reps": a.reps, "tune": keys,

@@ -156,24 +156,90 @@ __global__ void __launch_bounds__(256) velten_confocal_kernel(Grid g, int b, int
 // voxels, each thread VZ voxels 4 apart in z (default VZ = 4: 42.7 ms against
 // 51.1 ms for one voxel per thread and 46.3 ms for 8 on 128^3 voxels x 16,384
 // points, as the staged window and each scan point's shared-memory load serve
-// more voxels), scan points in tiles of 32. Per tile, warp 0 bounds the bins the block can reach from each
-// point (distance from the point to the block's box, one bin of margin each
-// side) and the CTA stages the union of those rows of the tile's 32 transient
-// columns in shared memory with coalesced 128-byte row reads (row stride 33,
-// so lanes reading different bins of one column hit different banks). Voxels
-// then read their bin from shared memory; a bin outside the staged rows (or a
-// tile whose rows exceed kWinRows) is read from global memory, so the window
+// more voxels), scan points in tiles of 32. Per tile, warp 0 bounds the bins
+// the block can reach from each point (distance from the point to the block's
+// box, one bin of margin each side) and the CTA stages the union of those
+// rows of the tile's 32 transient columns in shared memory with coalesced
+// 128-byte row reads (row stride 33, so lanes reading different bins of one
+// column hit different banks). Voxels then read their bin from shared memory;
+// a bin outside the staged rows is read from global memory, so the window
 // only affects speed. The sum runs over the scan points in the same order as
 // velten_confocal_kernel, so the two give identical volumes.
+//
+// A tile whose union exceeds kWinRows (fine bins: the union of 32 points
+// spans 2-4x the rows of 8 consecutive points) stages per group of
+// consecutive points instead: 4 groups of 8, whose 8 columns of a row are one
+// full 32-byte sector, when every group's union fits its part of the window;
+// else 8 groups of 4; else one window per point, cut to its first rows. With
+// one union per tile, 4,096 bins of 1.25 mm over 128^3 voxels from 128x128
+// points took 4.6x the time of 1,024 bins. The group windows are compiled
+// in only with kGrouped: their code alone, never taken, made the kernel 10%
+// slower at 1,024 bins (38.3 -> 42.8 ms), so the host launches them when a
+// point's bins over the voxel block alone span more than about 100 rows.
 constexpr int kBX = 8, kBY = 8, kBZ = 4, kST = 32, kWinRows = 256;
+constexpr int kWinFloats = kWinRows * (kST + 1);
 
-template <int VZ, int kOcc = 1>
+// rows of a bin span [lo, hi]; an empty span (lo = INT_MAX, hi = INT_MIN)
+// has none, and its difference is never formed (it overflows)
+__device__ __forceinline__ int span_rows(int lo, int hi) { return hi >= lo ? hi - lo + 1 : 0; }
+
+// Group windows: group g of COLS points holds rows [grp[g].x, grp[g].x +
+// grp[g].y) of its columns at win + g REGION, row stride STRIDE (COLS + 1,
+// odd, for COLS > 1). REGION = COLS mod 32, so one row of all groups, as
+// staged, lands on 32 distinct banks; 4 x 2088, 8 x 1028 and 32 x 257 floats
+// fit kWinFloats.
+template <int COLS, int STRIDE, int REGION>
+__device__ __forceinline__ void velten_group_stage(float* win, const int2* grp, int cnt, int rows_max,
+                                                   const float* __restrict__ trb, int S, int s0) {
+  const int k = threadIdx.x & 31;  // a warp stages one row of every group
+  const int2 d = grp[k / COLS];
+  const int rows = k < cnt ? d.y : 0;
+  float* dst = win + (k / COLS) * REGION + k % COLS;
+  for (int r = threadIdx.x >> 5; r < rows_max; r += blockDim.x >> 5)
+    if (r < rows) dst[r * STRIDE] = __ldg(trb + (size_t)(d.x + r) * S + s0 + k);
+}
+
+// The samples of a tile with group windows. Points j >= cnt of a partial
+// tile carry a NaN distance, whose bin (-1) is neither staged nor in [0, T):
+// they add nothing.
+template <int COLS, int STRIDE, int REGION, int VZ>
+__device__ __forceinline__ void velten_group_samples(const float* win, const float4* pts,
+                                                     const int2* grp, const fv3 (&p)[VZ],
+                                                     float (&value)[VZ], int cnt, int T, int S,
+                                                     int s0, float bw, float bo, float inv_bw,
+                                                     float nbo, float half_m,
+                                                     const float* __restrict__ trb) {
+  for (int j0 = 0; j0 < cnt; j0 += COLS) {
+    const int2 d = grp[j0 / COLS];
+    const float* wg = win + (j0 / COLS) * REGION;
+#pragma unroll 1
+    for (int c = 0; c < COLS; ++c) {
+      const float4 q = pts[j0 + c];
+      const float dx = q.x - p[0].x, dy = q.y - p[0].y;
+      const float r2 = fmaf(dx, dx, dy * dy);
+#pragma unroll
+      for (int v = 0; v < VZ; ++v) {
+        const int t = velten_bin_col(mkv(q.x, q.y, q.z), q.w, p[v], r2, bw, bo, inv_bw, nbo,
+                                     half_m);
+        const unsigned r = (unsigned)t - (unsigned)d.x;
+        if (r < (unsigned)d.y) value[v] += wg[r * STRIDE + c];
+        else if ((unsigned)t < (unsigned)T)
+          value[v] += __ldg(trb + (size_t)t * S + s0 + j0 + c);
+      }
+    }
+  }
+}
+
+template <int VZ, int kOcc = 1, bool kGrouped = false>
 __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
     Grid g, int b, int T, int S, Pts3 sp, Pts3 so, int has_origin, float bw, float bo,
     FastBin fb, const float* __restrict__ tr, float* __restrict__ vol) {
-  __shared__ float win[kWinRows * (kST + 1)];
+  __shared__ float win[kWinFloats];
   __shared__ float4 pts[kST];
+  __shared__ int2 grp[kST];  // group windows: first staged bin, staged rows
   __shared__ int span[2];
+  __shared__ int tile_cols;  // 32: one window; 8, 4, 1: points per group window
+  __shared__ int tile_rows;  // group windows: the most rows any group stages
   __shared__ float tile_margin;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x0 = blockIdx.x * kBX, y0 = blockIdx.y * kBY, z0 = blockIdx.z * kBZ * VZ;
@@ -204,10 +270,11 @@ __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
     if (warp == 0) {
       int tlo = INT_MAX, thi = INT_MIN;
       float mrg = 0.f;  // margin bound of this lane's pairs (infinite: exact chain)
+      float4 pt = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7fc00000));  // NaN distance
       if (lane < cnt) {
         const fv3 q = sp.at(b, s0 + lane);
         const float od2 = xmul(2.f, has_origin ? xlen(xsub3(q, so.at(b, s0 + lane))) : 0.f);
-        pts[lane] = make_float4(q.x, q.y, q.z, od2);
+        pt = make_float4(q.x, q.y, q.z, od2);
         const float ex = fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.f);
         const float ey = fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.f);
         const float ez = fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.f);
@@ -227,34 +294,63 @@ __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
         mrg = 1.02f * (fmaf(fb.k1, fabsf(dmax), fb.k2) + 1e-6f * cabs);
         if (!(mrg == mrg) || !(cabs < 2097152.f)) mrg = INFINITY;  // 2^21: rint range
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        tlo = min(tlo, __shfl_xor_sync(0xffffffffu, tlo, o));
-        thi = max(thi, __shfl_xor_sync(0xffffffffu, thi, o));
-        mrg = fmaxf(mrg, __shfl_xor_sync(0xffffffffu, mrg, o));
+      if (kGrouped || lane < cnt) pts[lane] = pt;
+      const int lo1 = tlo, hi1 = thi;
+      int lo4 = 0, hi4 = 0, lo8 = 0, hi8 = 0;
+      if constexpr (kGrouped) {
+        // unions of aligned groups of 4, 8 and 32 lanes (each within [0, T) or empty)
+        for (int o = 1; o < 32; o <<= 1) {
+          tlo = min(tlo, __shfl_xor_sync(0xffffffffu, tlo, o));
+          thi = max(thi, __shfl_xor_sync(0xffffffffu, thi, o));
+          mrg = fmaxf(mrg, __shfl_xor_sync(0xffffffffu, mrg, o));
+          if (o == 2) lo4 = tlo, hi4 = thi;
+          if (o == 4) lo8 = tlo, hi8 = thi;
+        }
+      } else {
+        for (int o = 16; o > 0; o >>= 1) {
+          tlo = min(tlo, __shfl_xor_sync(0xffffffffu, tlo, o));
+          thi = max(thi, __shfl_xor_sync(0xffffffffu, thi, o));
+          mrg = fmaxf(mrg, __shfl_xor_sync(0xffffffffu, mrg, o));
+        }
+      }
+      constexpr int kR8 = 232, kR4 = 205, kR1 = 257;  // rows of 2088 / 9, 1028 / 5, 257
+      int cols = 32, grows = 0;
+      if (kGrouped && span_rows(tlo, thi) > kWinRows) {
+        int glo;
+        if (__all_sync(0xffffffffu, span_rows(lo8, hi8) <= kR8))
+          cols = 8, glo = lo8, grows = span_rows(lo8, hi8);
+        else if (__all_sync(0xffffffffu, span_rows(lo4, hi4) <= kR4))
+          cols = 4, glo = lo4, grows = span_rows(lo4, hi4);
+        else
+          cols = 1, glo = lo1, grows = min(span_rows(lo1, hi1), kR1);
+        if ((lane & (cols - 1)) == 0) grp[lane / cols] = make_int2(glo, grows);
+        for (int o = 16; o > 0; o >>= 1) grows = max(grows, __shfl_xor_sync(0xffffffffu, grows, o));
       }
       if (lane == 0) {
         span[0] = tlo;
         span[1] = thi;
+        tile_cols = cols;
+        tile_rows = grows;
         tile_margin = mrg;
       }
     }
     __syncthreads();
-    // an empty window leaves tlo = INT_MAX, thi = INT_MIN: no rows (the
-    // difference must not be formed, it overflows)
-    const int tlo = span[0], thi = span[1];
-    const int rows = (tlo >= 0 && thi < T && thi >= tlo) ? thi - tlo + 1 : 0;
-    const bool staged = rows > 0 && rows <= kWinRows;
-    if (staged)
-      for (int i = threadIdx.x; i < rows * kST; i += blockDim.x) {
-        const int r = i >> 5, c = i & 31;
-        win[r * (kST + 1) + c] = c < cnt ? __ldg(trb + (size_t)(tlo + r) * S + s0 + c) : 0.f;
-      }
-    __syncthreads();
-    {
-      // one unsigned compare accepts a staged row (the window lies in [0, T));
-      // anything else is read from global memory if it is a bin at all.
-      // Voxels past the volume's edge compute on a clamped position and are
-      // never written.
+    // one unsigned compare accepts a staged row (the windows lie in [0, T));
+    // anything else is read from global memory if it is a bin at all. Voxels
+    // past the volume's edge compute on a clamped position and are never
+    // written.
+    const int cols = tile_cols;
+    if (!kGrouped || cols == 32) {
+      // (with kGrouped a tile takes this path only when its union fits)
+      const int tlo = span[0], thi = span[1];
+      const int rows = (tlo >= 0 && thi < T && thi >= tlo) ? thi - tlo + 1 : 0;
+      const bool staged = rows > 0 && rows <= kWinRows;
+      if (staged)
+        for (int i = threadIdx.x; i < rows * kST; i += blockDim.x) {
+          const int r = i >> 5, c = i & 31;
+          win[r * (kST + 1) + c] = c < cnt ? __ldg(trb + (size_t)(tlo + r) * S + s0 + c) : 0.f;
+        }
+      __syncthreads();
       const unsigned srows = staged ? (unsigned)rows : 0u;
       const float half_m = 0.5f - tile_margin;
       for (int j = 0; j < cnt; ++j) {
@@ -270,6 +366,24 @@ __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
           else if ((unsigned)t < (unsigned)T) value[v] += __ldg(trb + (size_t)t * S + s0 + j);
         }
       }
+    } else if (cols == 8) {
+      velten_group_stage<8, 9, 2088>(win, grp, cnt, tile_rows, trb, S, s0);
+      __syncthreads();
+      const float half_m = 0.5f - tile_margin;
+      velten_group_samples<8, 9, 2088>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+                                       fb.nbo, half_m, trb);
+    } else if (cols == 4) {
+      velten_group_stage<4, 5, 1028>(win, grp, cnt, tile_rows, trb, S, s0);
+      __syncthreads();
+      const float half_m = 0.5f - tile_margin;
+      velten_group_samples<4, 5, 1028>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+                                       fb.nbo, half_m, trb);
+    } else {
+      velten_group_stage<1, 1, 257>(win, grp, cnt, tile_rows, trb, S, s0);
+      __syncthreads();
+      const float half_m = 0.5f - tile_margin;
+      velten_group_samples<1, 1, 257>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+                                      fb.nbo, half_m, trb);
     }
   }
 #pragma unroll
@@ -486,6 +600,22 @@ int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
     return fail(TOTRI_ERR_INVALID_ARGUMENT, "backprojection.velten.vz must be 1, 2 or 4");
   const dim3 grid((unsigned)ceil_div(g.W, bp::kBX), (unsigned)ceil_div(g.H, bp::kBY),
                   (unsigned)ceil_div(g.D, bp::kBZ * vz));
+  // Group windows when one point's bins over a voxel block alone, 2 |block
+  // diagonal| / bw, span more than 100 rows (measured on 128^3 and 192^3
+  // voxels from 128^2 and 256^2 points: whole-tile windows were faster up to
+  // 82 rows, group windows from 122); "backprojection.velten.groups" = 1
+  // forces whole-tile windows, 2 group windows.
+  int groups = tune::get("backprojection.velten.groups");
+  if (groups != 1 && groups != 2) {
+    const auto pitch = [](float a, float e, int n) {
+      return n > 1 ? std::fabs((double)e - (double)a) / (n - 1) : 0.0;
+    };
+    const double ex = bp::kBX * pitch(g.sx, g.ex, g.W), ey = bp::kBY * pitch(g.sy, g.ey, g.H);
+    const double ez = bp::kBZ * vz * pitch(g.sz, g.ez, g.D);
+    const double rows = 2.0 * std::sqrt(ex * ex + ey * ey + ez * ez) / std::fabs((double)bw);
+    groups = rows > 100.0 ? 2 : 1;
+  }
+  const bool grouped = groups == 2;
   for (int b = 0; b < (int)B; ++b) {
     const bp::FastBin fb = bp::make_fast_bin(bw, bo);
     const float* trp = static_cast<const float*>(transient->data);
@@ -494,22 +624,23 @@ int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
     // spills; 34 KB of shared memory each): 38.2 ms against 40.4 ms uncapped
     // (47 registers, 5 CTAs; "backprojection.velten.occupancy" = 1), the same
     // volume bit for bit.
+#define TOTRI_VELTEN_TILED(VZ, OCC)                                                        \
+  TOTRI_KERNEL("backprojection velten confocal", stream,                                  \
+               grouped ? (bp::velten_confocal_tiled_kernel<VZ, OCC, true>                 \
+                          <<<grid, 256, 0, stream>>>(g, b, T, (int)S, sp, so, So > 0, bw, \
+                                                     bo, fb, trp, volp))                  \
+                       : (bp::velten_confocal_tiled_kernel<VZ, OCC, false>                \
+                          <<<grid, 256, 0, stream>>>(g, b, T, (int)S, sp, so, So > 0, bw, \
+                                                     bo, fb, trp, volp)))
     if (tiled && vz == 4 && tune::get("backprojection.velten.occupancy") != 1)
-      TOTRI_KERNEL("backprojection velten confocal", stream,
-                   (bp::velten_confocal_tiled_kernel<4, 6><<<grid, 256, 0, stream>>>(
-                       g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp)));
+      TOTRI_VELTEN_TILED(4, 6);
     else if (tiled && vz == 4)
-      TOTRI_KERNEL("backprojection velten confocal", stream,
-                   bp::velten_confocal_tiled_kernel<4><<<grid, 256, 0, stream>>>(
-                       g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp));
+      TOTRI_VELTEN_TILED(4, 1);
     else if (tiled && vz == 2)
-      TOTRI_KERNEL("backprojection velten confocal", stream,
-                   bp::velten_confocal_tiled_kernel<2><<<grid, 256, 0, stream>>>(
-                       g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp));
+      TOTRI_VELTEN_TILED(2, 1);
     else if (tiled)
-      TOTRI_KERNEL("backprojection velten confocal", stream,
-                   bp::velten_confocal_tiled_kernel<1><<<grid, 256, 0, stream>>>(
-                       g, b, T, (int)S, sp, so, So > 0, bw, bo, fb, trp, volp));
+      TOTRI_VELTEN_TILED(1, 1);
+#undef TOTRI_VELTEN_TILED
     else
       TOTRI_KERNEL("backprojection velten confocal", stream,
                    bp::velten_confocal_kernel<<<(unsigned)ceil_div(nv, 256), 256, 0, stream>>>(

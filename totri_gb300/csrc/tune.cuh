@@ -30,8 +30,10 @@
 //                               atomics, 2 lane-owned cells (up to 256 cells)
 //   "volume.adjoint.warps"      warps per CTA of the lanes-over-columns adjoint
 //   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
-//   "backprojection.velten.mode", ".occupancy", ".vz"
-//                               Velten kernel variant, 1: uncapped registers, slab depth
+//   "backprojection.velten.mode", ".occupancy", ".vz", ".groups"
+//                               Velten kernel variant, 1: uncapped registers, slab depth,
+//                               bin windows (1 one per tile, 2 per point group; 0: by the
+//                               voxel block's span in bins)
 //   "rbf.cull"                  1: RBF kernels without the underflow cull
 #pragma once
 
