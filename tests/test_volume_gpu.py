@@ -298,3 +298,24 @@ def test_adjoint_columns_kernel_block_shapes(cuda_lib, warps):
     finally:
         autotune.set_tile("volume.adjoint.warps", 0)
     assert rel(adj.cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("slabs", [1, 2, 3, 7])
+def test_adjoint_columns_kernel_slabs(cuda_lib, slabs):
+    """The lanes-over-columns adjoint with its columns whole or split into z
+    slabs of cells, a CTA per slab ("volume.adjoint.slabs"; slabs that do not
+    divide the column, sample pairs straddling two slabs), against the FP64
+    exact adjoint: lifted points (columns that start below a point) and a
+    negative bin offset."""
+    from totri_gb300 import autotune
+    for Z, bo in ((100, 0.0), (48, -1.0), (19, 0.0)):
+        vol, mp, org, size, T, bw, bo = column_case(Z, seed=Z + slabs, bo=bo, lift=True)
+        y = np.random.default_rng(Z + 3).standard_normal((mp.shape[1], T)).astype(np.float32)
+        ref = oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo)
+        autotune.set_tile("volume.adjoint.slabs", slabs)
+        try:
+            adj = torch.full(vol.shape, 7.0, device="cuda")
+            R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+        finally:
+            autotune.set_tile("volume.adjoint.slabs", 0)
+        assert rel(adj.cpu().numpy(), ref) < 1e-5

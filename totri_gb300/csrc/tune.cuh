@@ -29,6 +29,7 @@
 //   "volume.adjoint.mode"       0 lanes over 32 columns (default), 1 shared-memory
 //                               atomics, 2 lane-owned cells (up to 256 cells)
 //   "volume.adjoint.warps"      warps per CTA of the lanes-over-columns adjoint
+//   "volume.adjoint.slabs"      z slabs of its columns (default: slabs of <= 64 cells)
 //   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
 //   "backprojection.velten.mode", ".occupancy", ".vz", ".groups"
 //                               Velten kernel variant, 1: uncapped registers, slab depth,

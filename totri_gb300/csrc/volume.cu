@@ -528,6 +528,8 @@ __global__ void __launch_bounds__(256) confocal_adjoint_cells_kernel(Geo g, Poin
 }
 
 constexpr int kAdjUnroll = 4;  // bins per step of the lanes-over-columns adjoint
+// (8 bins per step, at 80 registers, measured the same: 65.6 against 65.8 ms)
+constexpr int kAdjTablePad = kAdjUnroll;  // table entries past the last bin
 
 // The bins [t0, t1] of one point for the lanes' columns, kAdjUnroll at a time:
 // the fast path without branches (a sample that is not taken adds zero to
@@ -540,23 +542,23 @@ constexpr int kAdjUnroll = 4;  // bins per step of the lanes-over-columns adjoin
 // the other walk) bins past t1 are skipped. z_hat = (depth + (wz - oz)) scale
 // - 0.5: the rounding of either association is inside sample_filtered's
 // margin.
-template <bool kCheck>
+template <bool kCheck, int U>
 __device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict__ tab,
                                          const float* __restrict__ row, float* col, int t0,
                                          int t1, int lane, float ddx, float ddy, float wz,
                                          float wzo, float pm, float wx, float wy, float x,
-                                         float y) {
+                                         float y, int za, int zn) {
   const int tend = kCheck ? t1 : g.T - 1;  // last bin whose value is read
   float wval = 0.f;                        // bin t0 + 32 k + lane
-  for (int t = t0; t <= t1; t += kAdjUnroll) {
+  for (int t = t0; t <= t1; t += U) {
     const int wo = (t - t0) & 31;
     if (wo == 0) wval = t + lane <= tend ? __ldg(row + t + lane) : 0.f;
-    int zi[kAdjUnroll];
-    float w0[kAdjUnroll], w1[kAdjUnroll];
-    bool slow[kAdjUnroll];
+    int zi[U];
+    float w0[U], w1[U];
+    bool slow[U];
     bool any_slow = false;
 #pragma unroll
-    for (int q = 0; q < kAdjUnroll; ++q) {
+    for (int q = 0; q < U; ++q) {
       const float val = __shfl_sync(0xffffffffu, wval, wo + q);
       const float2 tb = (!kCheck || t + q <= t1) ? tab[t + q] : make_float2(-INFINITY, 0.f);
       const float d2 = xsub(xsub(tb.x, ddx), ddy);
@@ -567,9 +569,9 @@ __device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict_
       const float fr = zh - fl;
       const bool fast = !g.exact && fabsf(fr - 0.5f) < 0.5f - pm;
       const int z = __float2int_rz(fl);
-      const bool ok = valid && fast && (unsigned)z < (unsigned)(g.Z - 1);
+      const bool ok = valid && fast && (unsigned)(z - za) < (unsigned)zn;
       const float v = val * ((d2 * d2) * tb.y);
-      zi[q] = ok ? z : 0;
+      zi[q] = ok ? z - za : 0;
       w0[q] = ok ? (1.f - fr) * v : 0.f;
       w1[q] = ok ? fr * v : 0.f;
       slow[q] = valid && !fast;
@@ -577,19 +579,19 @@ __device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict_
     }
     if (__any_sync(0xffffffffu, any_slow)) {
 #pragma unroll
-      for (int q = 0; q < kAdjUnroll; ++q) {
+      for (int q = 0; q < U; ++q) {
         if (!slow[q]) continue;
         const Sample sm = sample(g, wx, wy, wz, t + q, x, y);
-        if (sm.ok) {
+        if (sm.ok && (unsigned)(sm.zi - za) < (unsigned)zn) {
           const float vv = __ldg(row + t + q) * sm.f2;
-          zi[q] = sm.zi;
+          zi[q] = sm.zi - za;
           w0[q] = (1.f - sm.alpha) * vv;
           w1[q] = sm.alpha * vv;
         }
       }
     }
 #pragma unroll
-    for (int q = 0; q < kAdjUnroll; ++q) {
+    for (int q = 0; q < U; ++q) {
       col[zi[q] * 32] += w0[q];
       col[zi[q] * 32 + 32] += w1[q];
     }
@@ -602,11 +604,14 @@ __device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict_
 // per coalesced load, handed out by shuffles), and the bin's tc^2 (the sample
 // chain's FP32 value) and 1 / tc^8 come from a per-CTA table in shared memory
 // (broadcast reads), so f2 = (depth / tc^2)^4 = d2^2 / tc^8 needs no second
-// special-function op. Each lane owns its column's cells in shared memory
-// ([cell][lane]: no bank conflicts, no atomics), one copy per warp; the warps
-// of a CTA take interleaved runs of 32 points of one point group, and the CTA
-// adds its summed columns into the volume (which the launcher zeroes) with
-// one atomic per cell when there is more than one group. Four bins per step,
+// special-function op. A CTA takes one slab of the columns' cells (the
+// samples whose cell pair starts there; the pair's second cell may be the next
+// slab's first, one extra row), and each lane owns its column's cells of the
+// slab in shared memory ([cell][lane]: no bank conflicts, no atomics), one
+// copy per warp; the warps of a CTA take interleaved runs of 32 points of one
+// point group, and the CTA adds its summed columns into the volume (which the
+// launcher zeroes) with one atomic per cell when there is more than one group
+// or slab. A point's bins are those whose samples can land in the slab. Four bins per step,
 // evaluated without branches, give each lane four independent sample chains
 // (a branchy two-bin version issued 52 warp instructions per sample at 46% of
 // issue slots, latency-bound with 12 warps per SM). The bins walked for a point
@@ -614,18 +619,24 @@ __device__ __forceinline__ void adj_walk(const Geo& g, const float2* __restrict_
 // in its own span, and a sample outside it is decided (and rejected) like any
 // other, so each (column, point, bin) is counted once. Decisions are the exact
 // chain's (sample_filtered's margin, taken over the largest |tc| of the union).
+template <int U>
 __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
     Geo g, Points mp, int N, int points_per_group, const float* __restrict__ tr,
-    float* __restrict__ vol, int accumulate) {
-  extern __shared__ float acc[];  // [warp][Z][32], then the bin table
+    float* __restrict__ vol, int accumulate, int slab) {
+  // slab blockIdx.z: the samples in cells [za, za + zn) (cell pairs (z, z + 1)
+  // with z < Z - 1), held in rows 0 .. slab of the column copies (row slab is
+  // cell za + slab, the next slab's first)
+  const int za = blockIdx.z * slab, zb = min(g.Z, za + slab), zn = min(zb, g.Z - 1) - za;
+  const int rows = slab + 1;
+  extern __shared__ float acc[];  // [warp][rows][32], then the bin table
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  float2* tab = reinterpret_cast<float2*>(acc + (size_t)nw * g.Z * 32);  // [T]: tc^2, 1/tc^8
+  float2* tab = reinterpret_cast<float2*>(acc + (size_t)nw * rows * 32);  // [T]: tc^2, 1/tc^8
   const int tiles_y = (g.Y + 7) >> 3;
   const int ty = (blockIdx.x % tiles_y) * 8, tx = (blockIdx.x / tiles_y) * 4;
   const int yi = ty + (lane & 7), xi = tx + (lane >> 3);
   const bool live = xi < g.X && yi < g.Y;
-  for (int j = threadIdx.x; j < nw * g.Z * 32; j += blockDim.x) acc[j] = 0.f;
-  for (int t = threadIdx.x; t < g.T + kAdjUnroll; t += blockDim.x) {
+  for (int j = threadIdx.x; j < nw * rows * 32; j += blockDim.x) acc[j] = 0.f;
+  for (int t = threadIdx.x; t < g.T + kAdjTablePad; t += blockDim.x) {
     if (t >= g.T) {  // padding: no sample
       tab[t] = make_float2(-INFINITY, 0.f);
       continue;
@@ -636,7 +647,7 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
     tab[t] = make_float2(tc2, (i2 * i2) * (i2 * i2));
   }
   __syncthreads();
-  float* col = acc + (size_t)warp * g.Z * 32 + lane;
+  float* col = acc + (size_t)warp * rows * 32 + lane;
   const float x = centre(g.ox, g.sx, g.X, live ? xi : 0);
   const float y = centre(g.oy, g.sy, g.Y, live ? yi : 0);
   const float u = 5.9604645e-8f;
@@ -660,7 +671,11 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
       const float dx = xsub(wx, x), dy = xsub(wy, y);
       const float ddx = live ? xmul(dx, dx) : INFINITY, ddy = live ? xmul(dy, dy) : 0.f;
       Spans sp{1, 0, 1, 0};
-      if (live) sp = column_span(g, tz, dx * dx + dy * dy, wz);
+      float cl, ch;
+      if (live && zn > 0 &&
+          tc_bounds(dx * dx + dy * dy, wz, g.oz + ((float)za + 0.5f) / g.scale,
+                    g.oz + ((float)zb + 0.5f) / g.scale, cl, ch))
+        sp = tc_spans(g, tz, cl, ch, 1.f);
       // warp union of the lanes' spans
       const int p0 = __reduce_min_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p0 : INT_MAX);
       const int p1 = __reduce_max_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p1 : -1);
@@ -679,20 +694,22 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
                        4.f * u * zhmax + 1e-7f;
       const float* row = tr + (size_t)(base + j) * g.T;
       const float wzo = wz - g.oz;
-      adj_walk<false>(g, tab, row, col, p0, p1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y);
+      adj_walk<false, U>(g, tab, row, col, p0, p1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y,
+                         za, zn);
       if (n0 <= n1)  // warp-uniform: negative bin centres (a negative bin offset)
-        adj_walk<true>(g, tab, row, col, n0, n1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y);
+        adj_walk<true, U>(g, tab, row, col, n0, n1, lane, ddx, ddy, wz, wzo, pm, wx, wy, x, y,
+                          za, zn);
     }
   }
   __syncthreads();
-  // cell z of column l: the sum over the warps' copies (l fastest: no bank
-  // conflicts in the reads)
-  for (int jj = threadIdx.x; jj < g.Z * 32; jj += blockDim.x) {
-    const int z = jj >> 5, l = jj & 31;
+  // cell za + r of column l: the sum over the warps' copies (l fastest: no
+  // bank conflicts in the reads)
+  for (int jj = threadIdx.x; jj < rows * 32; jj += blockDim.x) {
+    const int r = jj >> 5, l = jj & 31, z = za + r;
     const int cy = ty + (l & 7), cx = tx + (l >> 3);
-    if (cx >= g.X || cy >= g.Y) continue;
+    if (cx >= g.X || cy >= g.Y || z >= g.Z) continue;
     float sum = 0.f;
-    for (int w = 0; w < nw; ++w) sum += acc[((size_t)w * g.Z + z) * 32 + l];
+    for (int w = 0; w < nw; ++w) sum += acc[((size_t)w * rows + r) * 32 + l];
     float* dst = vol + ((size_t)cx * g.Y + cy) * g.Z + z;
     if (accumulate) atomicAdd(dst, sum);
     else *dst = sum;
@@ -865,8 +882,18 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
   // lanes over columns: warps per CTA such that two CTAs' copies of 32
   // columns and the bin table fit an SM's shared memory
   // ("volume.adjoint.warps" overrides); bins beyond 4,096 take the atomic kernel
-  const size_t table = sizeof(float2) * ((size_t)T + volume::kAdjUnroll);
-  const size_t per_warp = (size_t)Z * 32 * sizeof(float);
+  const size_t table = sizeof(float2) * ((size_t)T + volume::kAdjTablePad);
+  // The columns split into slabs of at most 64 cells, a CTA per slab: each
+  // warp's column copy is then 65 rows (8.3 KB), and 3 CTAs of 8 warps share
+  // an SM (24 warps) instead of 2 of 6 with whole 128-cell columns. 128^3
+  // voxels x 16,384 points: 65.8 ms with 2 slabs, 75.4 ms with 1 and 72.5 ms
+  // with 4 (each slab walks the union of its lanes' bins, so thinner slabs
+  // walk more bins in all). "volume.adjoint.slabs" sets the count.
+  int slabs = (int)tune::get("volume.adjoint.slabs");
+  if (slabs <= 0) slabs = (int)ceil_div(Z, 64);
+  slabs = std::min(slabs, Z);
+  const int slab = (int)ceil_div(Z, slabs);
+  const size_t per_warp = (size_t)(slab + 1) * 32 * sizeof(float);
   int warps = T <= 4096 && table < 113 * 1024 ? (int)((113 * 1024 - table) / per_warp) : 0;
   if (tune::get("volume.adjoint.warps") > 0) warps = tune::get("volume.adjoint.warps");
   warps = std::min(warps, 8);
@@ -876,21 +903,24 @@ int totri_volume_confocal_adjoint(const totri_array_t* vol, const totri_array_t*
   }
   if (mode == 0 && warps >= 1 && T <= 4096) {
     const size_t smem = (size_t)warps * per_warp + table;
-    TOTRI_CUDA(tune::ensure_dynamic_smem(
-        reinterpret_cast<const void*>(volume::confocal_adjoint_columns_kernel), smem));
     const int64_t tiles = ceil_div(Y, 8) * ceil_div(X, 4);
     // point groups: about 16 CTAs per SM in all, each group at least four
     // runs of 32 points per warp
-    const int64_t want = std::max<int64_t>(1, (16 * tune::sm_count()) / tiles);
+    const int nslab = (int)ceil_div(Z, slab);
+    const int64_t want = std::max<int64_t>(1, (16 * tune::sm_count()) / (tiles * nslab));
     const int groups =
         (int)std::max<int64_t>(1, std::min<int64_t>(want, N / (128 * warps)));
     const int per = (int)(ceil_div(ceil_div(N, groups), 32) * 32);
     const int used = (int)ceil_div(N, per);
-    if (used > 1) TOTRI_CUDA(cudaMemsetAsync(vd, 0, sizeof(float) * numel(vol), stream));
+    const int accumulate = used > 1 || nslab > 1;
+    if (accumulate) TOTRI_CUDA(cudaMemsetAsync(vd, 0, sizeof(float) * numel(vol), stream));
+    const dim3 grid3((unsigned)tiles, (unsigned)used, (unsigned)nslab);
+    TOTRI_CUDA(tune::ensure_dynamic_smem(
+        reinterpret_cast<const void*>(volume::confocal_adjoint_columns_kernel<volume::kAdjUnroll>),
+        smem));
     TOTRI_KERNEL("volume confocal adjoint", stream,
-                 volume::confocal_adjoint_columns_kernel<<<dim3((unsigned)tiles, (unsigned)used),
-                                                           warps * 32, smem, stream>>>(
-                     g, pts, N, per, trd, vd, used > 1 ? 1 : 0));
+                 volume::confocal_adjoint_columns_kernel<volume::kAdjUnroll>
+                 <<<grid3, warps * 32, smem, stream>>>(g, pts, N, per, trd, vd, accumulate, slab));
     return TOTRI_OK;
   }
   if (Z <= 256 && mode == 2) {
