@@ -88,6 +88,16 @@ int totri_tune_get(const char* key);
 size_t totri_mesh_workspace(int64_t batch, int64_t num_verts, int64_t num_faces,
                             int64_t num_points);
 
+/* Optional extra scratch for totri_mesh_exhaustive_grad_verts(_reuse), no
+ * reference counterpart: given a workspace of at least
+ * totri_mesh_workspace(B, V, F, S + L) + this many bytes, the gradient reads
+ * transient_grad through bins-last copies ([s][l][t] order, one batch item and
+ * at most 2 GiB of scan points at a time) instead of in place; the results are
+ * the same up to FP32 summation order. 0 when one scan point's L x T floats
+ * exceed 2 GiB (the gradient then always reads in place). */
+size_t totri_mesh_exhaustive_grad_scratch(int64_t num_scan_points, int64_t num_laser_points,
+                                          int64_t num_bins);
+
 /* Replaces totri_cpp.render.mesh_confocal_forward
  * (src/render/mesh.h:10-18, src/render/mesh.cpp:9-20).
  * verts [B,V,3] f32, faces [B|1,F,3] i32/i64 (-1 padded: the first face with a

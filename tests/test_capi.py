@@ -37,6 +37,19 @@ def test_version_and_workspace_query(lib):
     assert lib.totri_mesh_workspace(1, 10, 0, 16) == 0
 
 
+def test_exhaustive_grad_scratch_query(lib):
+    """The exhaustive gradient's optional bins-last scratch: all scan points
+    when they fit 2 GiB, else whole 256-point tiles of them (or fewer points
+    when a tile does not fit), and none when one scan point's lasers x bins
+    exceed 2 GiB."""
+    assert lib.totri_mesh_exhaustive_grad_scratch(36, 9, 300) == 36 * 9 * 300 * 4 + 64  # aligned
+    assert lib.totri_mesh_exhaustive_grad_scratch(1024, 256, 2048) == 1024 * 256 * 2048 * 4
+    assert lib.totri_mesh_exhaustive_grad_scratch(4096, 256, 2048) == 1024 * 256 * 2048 * 4
+    assert lib.totri_mesh_exhaustive_grad_scratch(4096, 1000, 4096) == 131 * 1000 * 4096 * 4
+    assert lib.totri_mesh_exhaustive_grad_scratch(10, 200000, 4096) == 0
+    assert lib.totri_mesh_exhaustive_grad_scratch(0, 9, 300) == 0
+
+
 def _arr(shape, dtype=0, ptr=0x10000):
     from totri_gb300 import _lib
     a = _lib.Array()

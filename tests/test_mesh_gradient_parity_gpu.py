@@ -254,7 +254,12 @@ def test_exhaustive_large_forward_at_every_laser_tile(exhaustive_large, lt, keys
 
 
 _GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.mode": 2},
-                  {"mesh.exhaustive.grad.occupancy": 4}, {"mesh.exhaustive.grad.faces": 1},
+                  {"mesh.exhaustive.grad.occupancy": 4}, {"mesh.exhaustive.grad.layout": 2},
+                  {"mesh.exhaustive.grad.layout": 2, "mesh.exhaustive.grad.sslice": 7,
+                   "mesh.exhaustive.grad.lchunk": 5},
+                  {"mesh.exhaustive.grad.chunk": 7},
+                  {"mesh.exhaustive.grad.chunk": 32, "mesh.exhaustive.grad.lchunk": 5},
+                  {"mesh.exhaustive.grad.faces": 1},
                   {"mesh.exhaustive.grad.faces": 5}, {"mesh.exhaustive.grad.faces": 32},
                   {"mesh.exhaustive.grad.lchunk": 5}, {"mesh.exhaustive.grad.lchunk": 8},
                   {"mesh.exhaustive.grad.sslice": 7},
@@ -266,7 +271,8 @@ _GRAD_VARIANTS = [{}, {"mesh.exhaustive.grad.mode": 1}, {"mesh.exhaustive.grad.m
 def test_exhaustive_large_gradient_matches_fp64_oracle(exhaustive_large, keys):
     """The three gradient kernels (separable point records, the default;
     per-lane mask tests; compacted triples) and the point-record kernel's
-    register cap, faces-per-CTA and laser-chunk shapes (including counts that
+    register cap, its transient_grad read in place or through bins-last
+    copies of 7 or 32 scan points at a time, faces-per-CTA and laser-chunk shapes (including counts that
     do not divide the face or laser count) against the FP64 oracle."""
     w = exhaustive_large
     d, bd = w["d"], w["bd"]

@@ -85,6 +85,7 @@ _SIGNATURES = {
                            ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                            ctypes.POINTER(ctypes.c_int)],
     "totri_mesh_workspace": [_i64, _i64, _i64, _i64],
+    "totri_mesh_exhaustive_grad_scratch": [_i64, _i64, _i64],
     "totri_mesh_confocal_forward": [_ArrP] * 6 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_confocal_grad_verts": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz, _vp],
     "totri_mesh_confocal_grad_verts_reuse": [_ArrP] * 8 + [_flt, _flt, _int, _vp, _sz, _vp],
@@ -136,6 +137,7 @@ _RESTYPES = {
     "totri_version": ctypes.c_char_p,
     "totri_last_error": ctypes.c_char_p,
     "totri_mesh_workspace": ctypes.c_size_t,
+    "totri_mesh_exhaustive_grad_scratch": ctypes.c_size_t,
     "totri_mesh_mask_bytes": ctypes.c_size_t,
     "totri_volume_workspace": ctypes.c_size_t,
     "totri_marching_cubes_workspace": ctypes.c_size_t,

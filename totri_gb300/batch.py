@@ -101,7 +101,11 @@ class BatchedMeshRenderer:
             item = (T, S)
             points = S
         item_bytes = 4 * math.prod(item) * (1 if grad == "energy" else 2)
-        per_wave = max(1, int(hbm_budget // item_bytes))
+        # the exhaustive gradient's bins-last scratch (at most 2 GiB) comes
+        # out of the budget first
+        scratch = (int(self.lib.totri_mesh_exhaustive_grad_scratch(S, L, T))
+                   if self.exhaustive else 0)
+        per_wave = max(1, int((hbm_budget - scratch) // item_bytes))
         if grad == "external" and per_wave < len(meshes):
             raise ValueError("grad='external' needs the whole batch in one wave: %d meshes, "
                              "%d fit the HBM budget" % (len(meshes), per_wave))
@@ -126,7 +130,8 @@ class BatchedMeshRenderer:
         ws = max(int(self.lib.totri_mesh_workspace(len(w.members), w.verts.shape[1],
                                                    w.faces.shape[1], points))
                  for w in self.waves)
-        self.workspace = torch.empty(max(ws, 1), dtype=torch.uint8, device=dev)
+        # each wave's gradient finds the scratch past its own mesh layout
+        self.workspace = torch.empty(max(ws + scratch, 1), dtype=torch.uint8, device=dev)
         self.stream = torch.cuda.Stream(dev)
         self.tiles = {}
         if tune:

@@ -246,7 +246,8 @@ int exhaustive_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
   if (e.m.F == 0 || e.S == 0 || e.L == 0 || e.T == 0 || e.m.B == 0 || (!out.vg && !out.mg))
     return TOTRI_OK;
   const int64_t P = e.S + e.L;
-  TOTRI_TRY(check_workspace(ws, ws_bytes, mesh::layout(e.m.B, e.m.F, P).total));
+  const size_t base = mesh::layout(e.m.B, e.m.F, P).total;
+  TOTRI_TRY(check_workspace(ws, ws_bytes, base));
   const mesh::Scene sc = mesh::scene_from_workspace(ws, e.m.B, e.m.F, P);
   if (!reuse) {
     TOTRI_TRY(mesh::build_scene(sc, e.m.in, stream));
@@ -254,10 +255,13 @@ int exhaustive_grad_impl(const totri_array_t* verts, const totri_array_t* faces,
     TOTRI_TRY(
         mesh::launch_visibility(sc, view3f(laser_points), (int)e.L, (int)e.S, false, stream));
   }
+  // the bytes past the mesh layout (256-aligned) are the optional scratch
+  void* scratch = ws_bytes > base ? static_cast<char*>(ws) + base : nullptr;
   return mesh::launch_exhaustive_grad(sc, view3f(scan_points), view3f(laser_points), e.org,
                                       (int)e.S, (int)e.L,
                                       static_cast<const float*>(transient_grad->data), (int)e.T,
-                                      bw, bo, out, stream);
+                                      bw, bo, out, scratch, scratch ? ws_bytes - base : 0,
+                                      stream);
 }
 
 }  // namespace
@@ -276,6 +280,11 @@ size_t totri_mesh_workspace(int64_t batch, int64_t num_verts, int64_t num_faces,
   (void)num_verts;
   if (batch <= 0 || num_faces <= 0 || num_points < 0) return 0;
   return mesh::layout(batch, num_faces, num_points).total;
+}
+
+size_t totri_mesh_exhaustive_grad_scratch(int64_t num_scan_points, int64_t num_laser_points,
+                                          int64_t num_bins) {
+  return mesh::exh_grad_scratch_bytes(num_scan_points, num_laser_points, num_bins);
 }
 
 static int confocal_forward_impl(const totri_array_t* verts, const totri_array_t* faces,

@@ -13,6 +13,8 @@
 // walks every (s, l) pair of the slice.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "capi_common.cuh"
 #include "mesh.cuh"
 #include "mesh_kernels.cuh"
@@ -508,6 +510,9 @@ __global__ void __launch_bounds__(256) exh_grad_compact_kernel(
 // (vertex order, bins) are those of exh_pair.
 constexpr int kFaceSlice = 256;
 constexpr int kFacesPerCta = 8;
+// Most bytes of one bins-last copy of transient_grad (a range of scan points
+// of one batch item; launch_exhaustive_grad).
+constexpr size_t kGradChunkBytes = size_t(2) << 30;
 constexpr int kRec = 24;  // floats per point record (fields below)
 enum : int {
   kRecD = 0,     // [3] exact FP32 lengths
@@ -578,22 +583,28 @@ __device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* tota
 template <int kOcc>
 __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
     Scene sc, View3f sp, View3f lp, Origins org, int S, int L, const float* __restrict__ tgrad,
-    int T, float bw, float bo, GradOut out, int faces_per_cta, int lchunk, int sslice) {
+    int T, float bw, float bo, GradOut out, int faces_per_cta, int lchunk, int sslice, int b0,
+    int s_base, int s_end, int64_t bstride, int64_t cstep, int64_t bstep) {
+  // Batch item b0 + blockIdx.y, scan points [s_base, s_end); transient_grad
+  // element (t, s, l) of item b is tgrad[(b - b0) bstride + ((s - s_base) L +
+  // l) cstep + t bstep]: the caller's [B, T, S, L] tensor (b0 = s_base = 0,
+  // bstride = T S L, cstep = 1, bstep = S L) or one item's bins-last copy of
+  // a range of scan points (cstep = T, bstep = 1).
   extern __shared__ float recs[];        // scan-point then laser-point records, SoA
   float* srec = recs;
   float* lrec = recs + kRec * kFaceSlice;
   __shared__ short sidx[kFaceSlice], lidx[kFaceSlice];
   __shared__ int counts[2][8];
   __shared__ float red[8][10];
-  const int b = blockIdx.y;
+  const int b = b0 + blockIdx.y;
   const int n = sc.meta[b].n;
   const int nlc = (L + lchunk - 1) / lchunk;
-  const int s0 = (blockIdx.z / nlc) * sslice;
-  const int ns_all = min(sslice, S - s0);
+  const int s0 = s_base + (blockIdx.z / nlc) * sslice;
+  const int ns_all = min(sslice, s_end - s0);
   const int la = (blockIdx.z % nlc) * lchunk, lb = min(L, la + lchunk);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float* tgb = tgrad + (size_t)b * T * S * L;
-  const int64_t stride = (int64_t)S * L;
+  const float* tgb = tgrad + (int64_t)(b - b0) * bstride;
+  const int64_t stride = bstep;
   const float4* shade = sc.shade + (size_t)b * sc.F * 4;
   const uint32_t* mrows = sc.mask + (size_t)b * sc.P * sc.nch;
   const float inv_bw = __frcp_rn(bw);
@@ -679,7 +690,7 @@ __global__ void __launch_bounds__(256, kOcc) exh_grad_face_kernel(
         bin[1] = bin_of(xdiv(xsub(xadd(d1, od), bo), bw));
         bin[2] = bin_of(xdiv(xsub(xadd(d2, od), bo), bw));
         if (bin[0] >= T || bin[2] < 0) continue;
-        const float* col = tgb + (size_t)s * L + l;
+        const float* col = tgb + ((int64_t)(s - s_base) * L + l) * cstep;
         fv3 da[3];
         {
           const fv3 w = wf + mkv(rs[kRecWv * kFaceSlice], rs[(kRecWv + 1) * kFaceSlice],
@@ -869,9 +880,47 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
   return fail(TOTRI_ERR_UNSUPPORTED, "number of bins too large for the shared-memory tile");
 }
 
+// out[c][t] = in[t row + c] for c < n, t < T: a [T][n] block of rows of
+// length `row` into bins-last order, through 32 x 32 tiles in shared memory
+// (coalesced reads and writes).
+__global__ void __launch_bounds__(256) bins_last_kernel(const float* __restrict__ in,
+                                                        float* __restrict__ out, int T,
+                                                        int64_t row, int64_t n) {
+  __shared__ float tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32;
+  const int t0 = blockIdx.y * 32;
+  const float* src = in;
+  float* dst = out;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int t = t0 + r;
+    const int64_t c = c0 + threadIdx.x;
+    tile[r][threadIdx.x] = (t < T && c < n) ? src[(int64_t)t * row + c] : 0.f;
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int64_t c = c0 + r;
+    const int t = t0 + threadIdx.x;
+    if (t < T && c < n) dst[c * T + t] = tile[threadIdx.x][r];
+  }
+}
+
+int64_t exh_grad_chunk_points(int64_t S, int64_t L, int64_t T) {
+  if (S <= 0 || L <= 0 || T <= 0) return 0;
+  int64_t c = (int64_t)(kGradChunkBytes / ((size_t)L * (size_t)T * sizeof(float)));
+  if (c <= 0) return 0;
+  if (c >= S) return S;
+  return c >= kFaceSlice ? c / kFaceSlice * kFaceSlice : c;
+}
+
+size_t exh_grad_scratch_bytes(int64_t S, int64_t L, int64_t T) {
+  const int64_t c = exh_grad_chunk_points(S, L, T);
+  return c > 0 ? align_up((size_t)c * (size_t)L * (size_t)T * sizeof(float), 256) : 0;
+}
+
 int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                            const Origins& org, int S, int L, const float* tgrad, int T, float bw,
-                           float bo, const GradOut& out, cudaStream_t stream) {
+                           float bo, const GradOut& out, void* scratch, size_t scratch_bytes,
+                           cudaStream_t stream) {
   const FastBins fast = make_fast_bins(bw, bo, tune::get("mesh.exhaustive.exact") != 1);
   // At most 512 scan points per CTA: a warp walks one face over its slice and
   // then the next face over the same slice, re-reading the same transient_grad
@@ -890,39 +939,77 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
   if (mode != 1 && mode != 2) {
     // "mesh.exhaustive.grad.faces": faces per CTA (default 8);
     // "mesh.exhaustive.grad.occupancy" = 4: registers capped for 4 CTAs per SM
-    // (64, with spills) instead of 3 (80). Each CTA takes `sslice` scan points
-    // and `lchunk` lasers, faces varying fastest over the grid, so the CTAs
-    // that run together read the transient_grad rows of one (scan slice, laser
-    // chunk). When a bin row of transient_grad (S L floats) reaches 2 MB the
-    // per-pair cost grows (one 20k-face mesh, 2,048 bins: 0.23 ms per thousand
-    // pairs at 64x64 x 8x8 points, 0.36 at 64x64 x 16x16), and 128 scan points
-    // by 32 lasers per CTA recover part of it (378 -> 331 ms at 64x64 x 16x16;
-    // at 32x32 x 16x16 whole 256 x 256 tiles stay faster, 54.8 against
-    // 58.5 ms). "mesh.exhaustive.grad.sslice" / ".lchunk" override.
+    // (64, with spills) instead of 3 (80); "mesh.exhaustive.grad.sslice" /
+    // ".lchunk": scan points / lasers per CTA.
     const int fpc = tune::get("mesh.exhaustive.grad.faces") > 0
                         ? (int)tune::get("mesh.exhaustive.grad.faces")
                         : kFacesPerCta;
-    const bool wide_rows = (int64_t)S * L >= (int64_t)1 << 19;
-    int lchunk = tune::get("mesh.exhaustive.grad.lchunk");
-    if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = wide_rows ? 32 : kFaceSlice;
-    int sslice = tune::get("mesh.exhaustive.grad.sslice");
-    if (sslice <= 0 || sslice > kFaceSlice) sslice = wide_rows ? 128 : kFaceSlice;
     const bool occ4 = tune::get("mesh.exhaustive.grad.occupancy") == 4;
     const void* fn = occ4 ? reinterpret_cast<const void*>(exh_grad_face_kernel<4>)
                           : reinterpret_cast<const void*>(exh_grad_face_kernel<3>);
     const size_t smem = sizeof(float) * 2 * kRec * kFaceSlice;
     TOTRI_CUDA(tune::ensure_dynamic_smem(fn, smem));
-    const dim3 grid((unsigned)ceil_div(sc.F, fpc), (unsigned)sc.B,
-                    (unsigned)(ceil_div(S, sslice) * ceil_div(L, lchunk)));
-    if (occ4)
-      TOTRI_KERNEL("mesh exhaustive grad", stream,
-                   exh_grad_face_kernel<4><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk, sslice));
-    else
-      TOTRI_KERNEL("mesh exhaustive grad", stream,
-                   exh_grad_face_kernel<3><<<grid, 256, smem, stream>>>(
-                       sc, sp, lp, org, S, L, tgrad, T, bw, bo, out, fpc, lchunk, sslice));
-    return TOTRI_OK;
+    auto launch = [&](const float* tg, int lchunk, int sslice, int b0, int nb, int sa, int sb,
+                      int64_t bstride, int64_t cstep, int64_t bstep) -> int {
+      const dim3 grid((unsigned)ceil_div(sc.F, fpc), (unsigned)nb,
+                      (unsigned)(ceil_div(sb - sa, sslice) * ceil_div(L, lchunk)));
+      if (occ4)
+        TOTRI_KERNEL("mesh exhaustive grad", stream,
+                     exh_grad_face_kernel<4><<<grid, 256, smem, stream>>>(
+                         sc, sp, lp, org, S, L, tg, T, bw, bo, out, fpc, lchunk, sslice, b0, sa,
+                         sb, bstride, cstep, bstep));
+      else
+        TOTRI_KERNEL("mesh exhaustive grad", stream,
+                     exh_grad_face_kernel<3><<<grid, 256, smem, stream>>>(
+                         sc, sp, lp, org, S, L, tg, T, bw, bo, out, fpc, lchunk, sslice, b0, sa,
+                         sb, bstride, cstep, bstep));
+      return TOTRI_OK;
+    };
+    int lchunk = tune::get("mesh.exhaustive.grad.lchunk");
+    int sslice = tune::get("mesh.exhaustive.grad.sslice");
+    // Bins-last copies. A triple reads a few consecutive bins of its (s, l)
+    // column; in the caller's [T, S, L] order they lie S L floats apart, one
+    // L2 sector each, read one after another. When the workspace holds the
+    // scratch (totri_mesh_exhaustive_grad_scratch), each item's transient_grad
+    // is copied, one range of scan points at a time, into [s][l][t] order,
+    // where those bins share one or two sectors: one 20k-face mesh, 2,048
+    // bins, 16x16 laser points: 333 -> 189 ms at 64x64 scan points, 54.2 ->
+    // 51.0 ms at 32x32 (copies included), with whole 256 x 256 tiles.
+    // "mesh.exhaustive.grad.layout" = 2 reads transient_grad in place;
+    // "mesh.exhaustive.grad.chunk" caps the scan points per copy.
+    int64_t cpts = exh_grad_chunk_points(S, L, T);
+    const int64_t cap = tune::get("mesh.exhaustive.grad.chunk");
+    if (cap > 0) cpts = std::min(cpts, cap);
+    if (tune::get("mesh.exhaustive.grad.layout") != 2 && cpts > 0 && scratch &&
+        scratch_bytes >= (size_t)cpts * L * T * sizeof(float)) {
+      if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = kFaceSlice;
+      if (sslice <= 0 || sslice > kFaceSlice) sslice = kFaceSlice;
+      sslice = (int)std::min<int64_t>(sslice, cpts);
+      float* copy = static_cast<float*>(scratch);
+      const int64_t row = (int64_t)S * L;
+      for (int b = 0; b < sc.B; ++b)
+        for (int64_t sa = 0; sa < S; sa += cpts) {
+          const int64_t sb = std::min<int64_t>(S, sa + cpts), n = (sb - sa) * L;
+          TOTRI_KERNEL("mesh exhaustive grad layout", stream,
+                       bins_last_kernel<<<dim3((unsigned)ceil_div(n, 32), (unsigned)ceil_div(T, 32)),
+                                          dim3(32, 8), 0, stream>>>(
+                           tgrad + ((int64_t)b * T) * row + sa * L, copy, T, row, n));
+          TOTRI_TRY(launch(copy, lchunk, sslice, b, 1, (int)sa, (int)sb, 0, T, 1));
+        }
+      return TOTRI_OK;
+    }
+    // In place: each CTA takes `sslice` scan points and `lchunk` lasers,
+    // faces varying fastest over the grid, so the CTAs that run together
+    // read the transient_grad rows of one (scan slice, laser chunk). When a
+    // bin row of transient_grad (S L floats) reaches 2 MB the per-pair cost
+    // grows (one 20k-face mesh, 2,048 bins: 0.23 ms per thousand pairs at
+    // 64x64 x 8x8 points, 0.36 at 64x64 x 16x16), and 128 scan points by 32
+    // lasers per CTA recover part of it (378 -> 331 ms at 64x64 x 16x16; at
+    // 32x32 x 16x16 whole 256 x 256 tiles stay faster, 54.8 against 58.5 ms).
+    const bool wide_rows = (int64_t)S * L >= (int64_t)1 << 19;
+    if (lchunk <= 0 || lchunk > kFaceSlice) lchunk = wide_rows ? 32 : kFaceSlice;
+    if (sslice <= 0 || sslice > kFaceSlice) sslice = wide_rows ? 128 : kFaceSlice;
+    return launch(tgrad, lchunk, sslice, 0, sc.B, 0, S, (int64_t)T * S * L, 1, (int64_t)S * L);
   }
   if (mode == 1) {
     const size_t smem = sizeof(uint32_t) * (size_t)(S + L);

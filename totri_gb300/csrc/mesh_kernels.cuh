@@ -341,7 +341,12 @@ int launch_exhaustive_splat(const Scene& sc, const View3f& sp, const View3f& lp,
                             float bo, cudaStream_t stream);
 int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                            const Origins& org, int S, int L, const float* tgrad, int T, float bw,
-                           float bo, const GradOut& out, cudaStream_t stream);
+                           float bo, const GradOut& out, void* scratch, size_t scratch_bytes,
+                           cudaStream_t stream);
+// Scan points per bins-last copy of transient_grad (0: none fits), and the
+// scratch bytes those copies need.
+int64_t exh_grad_chunk_points(int64_t S, int64_t L, int64_t T);
+size_t exh_grad_scratch_bytes(int64_t S, int64_t L, int64_t T);
 
 int launch_mask_unsort(const Scene& sc, int P, uint32_t* out, cudaStream_t stream);
 int launch_confocal_splat(const Scene& sc, const View3f& sp, const View3f& so, int has_origin,

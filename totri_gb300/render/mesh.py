@@ -11,7 +11,7 @@ import typing
 import torch
 
 from .. import _lib
-from ..totri_cpp._common import mesh_workspace, ws_args
+from ..totri_cpp._common import exhaustive_grad_scratch, mesh_workspace, ws_args
 from ..types import BinDef
 from ..util.format import colors_of_verts, faces_of_verts, origin_of_wallpoints
 
@@ -132,7 +132,11 @@ class MeshRenderExhaustive(torch.autograd.Function):
         S, L = scan_points.shape[1], laser_points.shape[1]
         transient = torch.empty((B, bin_def.num, S, L), device=verts.device,
                                 dtype=torch.float32)
-        ws = mesh_workspace(B, V, F, S + L, verts.device)
+        # the backward reuses this workspace: room for its bins-last scratch
+        # when a gradient will be asked for
+        grads = ctx.needs_input_grad[0] or ctx.needs_input_grad[5]
+        ws = mesh_workspace(B, V, F, S + L, verts.device,
+                            exhaustive_grad_scratch(S, L, bin_def.num) if grads else 0)
         _run("totri_mesh_exhaustive_forward",
              (verts, faces, colors, scan_points, laser_points, scan_origin, laser_origin,
               transient), bin_def, ws, verts.device)

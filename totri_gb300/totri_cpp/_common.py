@@ -16,12 +16,18 @@ def finish_out(t, out):
         t.copy_(out)
 
 
-def mesh_workspace(B, V, F, P, device):
-    """Scratch for one mesh call (BVH + visibility masks), from the caching allocator."""
+def mesh_workspace(B, V, F, P, device, extra=0):
+    """Scratch for one mesh call (BVH + visibility masks, then `extra` bytes),
+    from the caching allocator."""
     n = int(_lib.load().totri_mesh_workspace(int(B), int(V), int(F), int(P)))
     if n == 0:
         return None
-    return torch.empty(n, dtype=torch.uint8, device=device)
+    return torch.empty(n + int(extra), dtype=torch.uint8, device=device)
+
+
+def exhaustive_grad_scratch(S, L, T):
+    """Bytes of the exhaustive gradient's optional bins-last scratch."""
+    return int(_lib.load().totri_mesh_exhaustive_grad_scratch(int(S), int(L), int(T)))
 
 
 # Status bits that report internal errors (a BVH search at its limit, an index

@@ -7,13 +7,15 @@ sm_103a kernels of libtotri_gb300.so on the current CUDA stream.
 import torch
 
 from .. import _lib
-from ._common import check_device_status, dense_out, finish_out, mesh_workspace, ws_args
+from ._common import (check_device_status, dense_out, exhaustive_grad_scratch, finish_out,
+                      mesh_workspace, ws_args)
 
 
-def _mesh_call(name, tensors, bw, bo, model, points):
+def _mesh_call(name, tensors, bw, bo, model, points, extra=0):
     lib = _lib.load()
     verts, faces = tensors[0], tensors[1]
-    ws = mesh_workspace(verts.shape[0], verts.shape[1], faces.shape[1], points, verts.device)
+    ws = mesh_workspace(verts.shape[0], verts.shape[1], faces.shape[1], points, verts.device,
+                        extra)
     st = getattr(lib, name)(*[_lib.array(t) for t in tensors], float(bw), float(bo), int(model),
                             *ws_args(ws), _lib.stream_of(verts.device))
     _lib.check(st)
@@ -90,7 +92,9 @@ def mesh_exhaustive_grad_verts(verts, faces, material, scan_points, laser_points
     _mesh_call("totri_mesh_exhaustive_grad_verts",
                (verts, faces, material, scan_points, laser_points, scan_origin, laser_origin,
                 transient_grad.contiguous(), verts_grad, material_grad),
-               bin_width, bin_offset, model, scan_points.shape[1] + laser_points.shape[1])
+               bin_width, bin_offset, model, scan_points.shape[1] + laser_points.shape[1],
+               exhaustive_grad_scratch(scan_points.shape[1], laser_points.shape[1],
+                                       transient_grad.shape[1]))
 
 
 def _vol_call(name, tensors, a3, b3, bw, bo, device, voxels=None):
