@@ -904,6 +904,14 @@ __global__ void __launch_bounds__(256) bins_last_kernel(const float* __restrict_
   }
 }
 
+int launch_bins_last(const float* in, float* out, int T, int64_t row, int64_t n,
+                     cudaStream_t stream) {
+  TOTRI_KERNEL("mesh grad layout", stream,
+               bins_last_kernel<<<dim3((unsigned)ceil_div(n, 32), (unsigned)ceil_div(T, 32)),
+                                  dim3(32, 8), 0, stream>>>(in, out, T, row, n));
+  return TOTRI_OK;
+}
+
 int64_t exh_grad_chunk_points(int64_t S, int64_t L, int64_t T) {
   if (S <= 0 || L <= 0 || T <= 0) return 0;
   int64_t c = (int64_t)(kGradChunkBytes / ((size_t)L * (size_t)T * sizeof(float)));
@@ -990,10 +998,8 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
       for (int b = 0; b < sc.B; ++b)
         for (int64_t sa = 0; sa < S; sa += cpts) {
           const int64_t sb = std::min<int64_t>(S, sa + cpts), n = (sb - sa) * L;
-          TOTRI_KERNEL("mesh exhaustive grad layout", stream,
-                       bins_last_kernel<<<dim3((unsigned)ceil_div(n, 32), (unsigned)ceil_div(T, 32)),
-                                          dim3(32, 8), 0, stream>>>(
-                           tgrad + ((int64_t)b * T) * row + sa * L, copy, T, row, n));
+          TOTRI_TRY(launch_bins_last(tgrad + ((int64_t)b * T) * row + sa * L, copy, T, row, n,
+                                     stream));
           TOTRI_TRY(launch(copy, lchunk, sslice, b, 1, (int)sa, (int)sb, 0, T, 1));
         }
       return TOTRI_OK;

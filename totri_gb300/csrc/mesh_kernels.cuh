@@ -343,6 +343,10 @@ int launch_exhaustive_grad(const Scene& sc, const View3f& sp, const View3f& lp,
                            const Origins& org, int S, int L, const float* tgrad, int T, float bw,
                            float bo, const GradOut& out, void* scratch, size_t scratch_bytes,
                            cudaStream_t stream);
+// out[c][t] = in[t row + c] for c < n, t < T (a block of transient rows into
+// bins-last order).
+int launch_bins_last(const float* in, float* out, int T, int64_t row, int64_t n,
+                     cudaStream_t stream);
 // Scan points per bins-last copy of transient_grad (0: none fits), and the
 // scratch bytes those copies need.
 int64_t exh_grad_chunk_points(int64_t S, int64_t L, int64_t T);
