@@ -169,7 +169,11 @@ struct Points {  // measurement points [3, N] with strides
   __device__ float at(int c, int i) const { return p[c * sc + i * sn]; }
 };
 
-__global__ void compact_kernel(const float* __restrict__ vol, int64_t n, uint32_t* list,
+// The occupied voxels of a [X][Y][Z] volume as records (column centre x, y,
+// value, cell k): the per-voxel decoding (two divisions of the index, two
+// correctly rounded divisions for the centres) is done once here instead of
+// once per (voxel, point) pair.
+__global__ void compact_kernel(Geo g, const float* __restrict__ vol, int64_t n, float4* recs,
                                uint32_t* count) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool occ = i < n && vol[i] != 0.f;
@@ -179,7 +183,14 @@ __global__ void compact_kernel(const float* __restrict__ vol, int64_t n, uint32_
   uint32_t base = 0;
   if (lane == __ffs(m) - 1) base = atomicAdd(count, (uint32_t)__popc(m));
   base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-  if (occ) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+  if (occ) {
+    const uint32_t lin = (uint32_t)i;
+    const int k = (int)(lin % g.Z);
+    const int yi = (int)((lin / g.Z) % g.Y), xi = (int)(lin / ((uint32_t)g.Z * g.Y));
+    recs[base + __popc(m & ((1u << lane) - 1u))] =
+        make_float4(centre(g.ox, g.sx, g.X, xi), centre(g.oy, g.sy, g.Y, yi), vol[i],
+                    __int_as_float(k));
+  }
 }
 
 constexpr int kPT = 8;  // points per CTA tile
@@ -187,8 +198,8 @@ constexpr int kPT = 8;  // points per CTA tile
 // Confocal forward: tile of kPT points x all occupied voxels -> rows of the
 // transient in shared memory -> coalesced row stores.
 __global__ void __launch_bounds__(256) confocal_forward_kernel(
-    Geo g, const float* __restrict__ vol, const uint32_t* __restrict__ list,
-    const uint32_t* __restrict__ count, Points mp, int N, float* __restrict__ out) {
+    Geo g, const float4* __restrict__ recs, const uint32_t* __restrict__ count, Points mp, int N,
+    float* __restrict__ out) {
   extern __shared__ float hist[];  // [kPT][T]
   const int i0 = blockIdx.x * kPT;
   for (int j = threadIdx.x; j < kPT * g.T; j += blockDim.x) hist[j] = 0.f;
@@ -201,11 +212,9 @@ __global__ void __launch_bounds__(256) confocal_forward_kernel(
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
     float* row = hist + pl * g.T;
     for (uint32_t v = threadIdx.x / kPT; v < nnz; v += blockDim.x / kPT) {
-      const uint32_t lin = __ldg(list + v);
-      const int k = (int)(lin % g.Z);
-      const int yi = (int)((lin / g.Z) % g.Y), xi = (int)(lin / ((uint32_t)g.Z * g.Y));
-      const float val = __ldg(vol + lin);
-      const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
+      const float4 rec = __ldg(recs + v);
+      const float x = rec.x, y = rec.y, val = rec.z;
+      const int k = __float_as_int(rec.w);
       const float rho2 = (wx - x) * (wx - x) + (wy - y) * (wy - y);
       const Spans sp = bin_range(g, tz, rho2, wz, k);
       for (int r = 0; r < 2; ++r) {
@@ -232,8 +241,7 @@ __global__ void __launch_bounds__(256) confocal_forward_kernel(
 // d transient / d measurement points (volume_cuda.cu:189-265) with the same
 // occupied-voxel scatter; one thread accumulates one point's gradient over a
 // share of the voxels, reduced across the kPT-strided threads in shared memory.
-__global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __restrict__ vol,
-                                                      const uint32_t* __restrict__ list,
+__global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float4* __restrict__ recs,
                                                       const uint32_t* __restrict__ count,
                                                       Points mp, int N,
                                                       const float* __restrict__ tg,
@@ -250,11 +258,9 @@ __global__ void __launch_bounds__(256) grad_mp_kernel(Geo g, const float* __rest
     const float wx = mp.at(0, i), wy = mp.at(1, i), wz = mp.at(2, i);
     const float* trow = tg + (size_t)i * g.T;
     for (uint32_t v = threadIdx.x / kPT; v < nnz; v += blockDim.x / kPT) {
-      const uint32_t lin = __ldg(list + v);
-      const int k = (int)(lin % g.Z);
-      const int yi = (int)((lin / g.Z) % g.Y), xi = (int)(lin / ((uint32_t)g.Z * g.Y));
-      const float val = __ldg(vol + lin);
-      const float x = centre(g.ox, g.sx, g.X, xi), y = centre(g.oy, g.sy, g.Y, yi);
+      const float4 rec = __ldg(recs + v);
+      const float x = rec.x, y = rec.y, val = rec.z;
+      const int k = __float_as_int(rec.w);
       const float rho2 = (wx - x) * (wx - x) + (wy - y) * (wy - y);
       const Spans sp = bin_range(g, tz, rho2, wz, k);
       for (int r = 0; r < 2; ++r) {
@@ -798,9 +804,10 @@ Geo make_geo(int X, int Y, int Z, const float* o, const float* s, float bw, floa
   return g;
 }
 
-size_t occupancy_bytes(int64_t nvox) { return align_up(sizeof(uint32_t) * (nvox + 64), 256); }
+// the count (in a 256-byte header), then one record per voxel
+size_t occupancy_bytes(int64_t nvox) { return align_up(256 + sizeof(float4) * nvox, 256); }
 
-int compact(const float* vol, int64_t n, void* ws, size_t ws_bytes, uint32_t** list,
+int compact(const Geo& g, const float* vol, int64_t n, void* ws, size_t ws_bytes, float4** recs,
             uint32_t** count, cudaStream_t stream) {
   const size_t need = occupancy_bytes(n);
   if (!ws || ws_bytes < need)
@@ -808,11 +815,11 @@ int compact(const float* vol, int64_t n, void* ws, size_t ws_bytes, uint32_t** l
                 "workspace of " + std::to_string(need) + " bytes required, got " +
                     std::to_string(ws_bytes));
   *count = static_cast<uint32_t*>(ws);
-  *list = *count + 64;
+  *recs = reinterpret_cast<float4*>(static_cast<char*>(ws) + 256);
   TOTRI_CUDA(cudaMemsetAsync(*count, 0, sizeof(uint32_t), stream));
   TOTRI_KERNEL("volume compact", stream,
                volume::compact_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, stream>>>(
-                   vol, n, *list, *count));
+                   g, vol, n, *recs, *count));
   return TOTRI_OK;
 }
 
@@ -842,17 +849,17 @@ int totri_volume_confocal_forward(const totri_array_t* vol, const totri_array_t*
   if (N == 0 || T == 0) return TOTRI_OK;
   const size_t smem = sizeof(float) * volume::kPT * T;
   if (smem > 200 * 1024) return fail(TOTRI_ERR_UNSUPPORTED, "too many bins for one tile");
-  uint32_t *list, *count;
-  TOTRI_TRY(compact(static_cast<const float*>(vol->data), numel(vol), ws, ws_bytes, &list,
+  const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
+  float4* recs;
+  uint32_t* count;
+  TOTRI_TRY(compact(g, static_cast<const float*>(vol->data), numel(vol), ws, ws_bytes, &recs,
                     &count, stream));
   TOTRI_CUDA(tune::ensure_dynamic_smem(
       reinterpret_cast<const void*>(volume::confocal_forward_kernel), smem));
-  const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
   TOTRI_KERNEL("volume confocal forward", stream,
                volume::confocal_forward_kernel<<<(unsigned)ceil_div(N, volume::kPT), 256, smem,
-                                                 stream>>>(
-                   g, static_cast<const float*>(vol->data), list, count, pts, N,
-                   static_cast<float*>(tr->data)));
+                                                 stream>>>(g, recs, count, pts, N,
+                                                           static_cast<float*>(tr->data)));
   return TOTRI_OK;
 }
 
@@ -989,13 +996,14 @@ int totri_volume_confocal_grad_measurement_points(const totri_array_t* mpg,
   TOTRI_TRY(check_contiguous(tg, "transient_grad"));
   const int T = (int)tg->shape[1];
   if (N == 0) return TOTRI_OK;
-  uint32_t *list, *count;
-  TOTRI_TRY(compact(static_cast<const float*>(vol->data), numel(vol), ws, ws_bytes, &list,
-                    &count, stream));
   const Geo g = make_geo(X, Y, Z, origin, size, bw, bo, T);
+  float4* recs;
+  uint32_t* count;
+  TOTRI_TRY(compact(g, static_cast<const float*>(vol->data), numel(vol), ws, ws_bytes, &recs,
+                    &count, stream));
   TOTRI_KERNEL("volume confocal grad points", stream,
                volume::grad_mp_kernel<<<(unsigned)ceil_div(N, volume::kPT), 256, 0, stream>>>(
-                   g, static_cast<const float*>(vol->data), list, count, pts, N,
+                   g, recs, count, pts, N,
                    static_cast<const float*>(tg->data), static_cast<float*>(mpg->data),
                    mpg->strides[0], mpg->strides[1]));
   return TOTRI_OK;
