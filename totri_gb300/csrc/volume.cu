@@ -153,14 +153,24 @@ __device__ __forceinline__ bool tc_bounds(float rho2, float wz, float zlo, float
   return true;
 }
 
-// Bins whose sample may fall in interpolation cells k-1 or k of a column
-// (conservative: one extra bin each side).
+// Bins whose sample may fall in interpolation cells k-1 or k of a column,
+// widened by eps bins: the bound of confocal_adjoint_cells_kernel on the FP32
+// rounding of the sample chain against this inverse (64 u of the largest
+// magnitudes over the bin width, plus 0.01, at most one bin), with the
+// largest |tc| of the walked bins at most ch plus one bin. One whole bin each
+// side walked about two more bins per (voxel, point) pair.
 __device__ __forceinline__ Spans bin_range(const Geo& g, int tz, float rho2, float wz, int k) {
   float cl, ch;
   if (!tc_bounds(rho2, wz, g.oz + ((float)k - 0.5f) / g.scale,
                  g.oz + ((float)k + 1.5f) / g.scale, cl, ch))
     return Spans{1, 0, 1, 0};
-  return tc_spans(g, tz, cl, ch, 1.f);
+  const float u = 5.9604645e-8f;
+  const float dmax = 1.001f * (ch + fabsf(g.bw));
+  const float zmax = fabsf(wz) + dmax;
+  const float eps = fminf(64.f * u * (dmax + fabsf(g.bo) + fabsf(wz) + zmax + fabsf(g.oz) +
+                                      fabsf(1.f / g.scale)) * g.inv_bw + 0.01f,
+                          1.f);
+  return tc_spans(g, tz, cl, ch, eps);
 }
 
 struct Points {  // measurement points [3, N] with strides
