@@ -360,3 +360,29 @@ def test_forward_keeps_every_sample_of_sparse_volumes(cuda_lib, seed):
     R.volume_confocal_grad_measurement_points(gm, cu(vol), cu(mp), cu(y), org, size, bw, bo)
     assert rel(gm.cpu().numpy(), oracle.volume_confocal_grad_mp(vol, mp, y, org, size, bw,
                                                                 bo)) < 1e-4
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_adjoint_keeps_every_sample_of_sparse_cotangents(cuda_lib, seed):
+    """A cotangent with a few nonzero bins: each cell of the adjoint then sums
+    a handful of samples, so one missing from a lane's walked bins (its span is
+    widened by a rounding bound, a small fraction of a bin) would show far past
+    the 1e-5 bound. Whole columns and slabs, lifted points, a negative bin
+    offset; against the FP64 exact adjoint."""
+    from totri_gb300 import autotune
+    vol, mp, org, size, T, bw, bo = column_case(int(60 + 30 * seed), seed=200 + seed,
+                                                bo=-0.5 if seed % 2 else 0.0, lift=True)
+    g = np.random.default_rng(300 + seed)
+    y = np.zeros((mp.shape[1], T), np.float32)
+    hot = g.random(y.shape) < 0.01
+    y[hot] = g.standard_normal(hot.sum()).astype(np.float32)
+    ref = oracle.volume_confocal_adjoint(y, vol.shape, mp, org, size, bw, bo)
+    assert (ref != 0).sum() > 50
+    for slabs in (1, 3):
+        autotune.set_tile("volume.adjoint.slabs", slabs)
+        try:
+            adj = torch.full(vol.shape, 7.0, device="cuda")
+            R.volume_confocal_adjoint(adj, cu(mp), cu(y), org, size, bw, bo)
+        finally:
+            autotune.set_tile("volume.adjoint.slabs", 0)
+        assert rel(adj.cpu().numpy(), ref) < 1e-5

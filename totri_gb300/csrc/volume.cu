@@ -153,24 +153,29 @@ __device__ __forceinline__ bool tc_bounds(float rho2, float wz, float zlo, float
   return true;
 }
 
-// Bins whose sample may fall in interpolation cells k-1 or k of a column,
-// widened by eps bins: the bound of confocal_adjoint_cells_kernel on the FP32
-// rounding of the sample chain against this inverse (64 u of the largest
+// The widening, in bins, of a span from tc_bounds whose largest centre
+// magnitude is ch: the bound of confocal_adjoint_cells_kernel on the FP32
+// rounding of the sample chain against that inverse (64 u of the largest
 // magnitudes over the bin width, plus 0.01, at most one bin), with the
-// largest |tc| of the walked bins at most ch plus one bin. One whole bin each
-// side walked about two more bins per (voxel, point) pair.
+// largest |tc| of the walked bins at most ch plus one bin.
+__device__ __forceinline__ float span_eps(const Geo& g, float ch, float wz) {
+  const float u = 5.9604645e-8f;
+  const float dmax = 1.001f * (ch + fabsf(g.bw));
+  const float zmax = fabsf(wz) + dmax;
+  return fminf(64.f * u * (dmax + fabsf(g.bo) + fabsf(wz) + zmax + fabsf(g.oz) +
+                           fabsf(1.f / g.scale)) * g.inv_bw + 0.01f,
+               1.f);
+}
+
+// Bins whose sample may fall in interpolation cells k-1 or k of a column,
+// widened by span_eps (a whole bin each side walked about two more bins per
+// (voxel, point) pair of the forward).
 __device__ __forceinline__ Spans bin_range(const Geo& g, int tz, float rho2, float wz, int k) {
   float cl, ch;
   if (!tc_bounds(rho2, wz, g.oz + ((float)k - 0.5f) / g.scale,
                  g.oz + ((float)k + 1.5f) / g.scale, cl, ch))
     return Spans{1, 0, 1, 0};
-  const float u = 5.9604645e-8f;
-  const float dmax = 1.001f * (ch + fabsf(g.bw));
-  const float zmax = fabsf(wz) + dmax;
-  const float eps = fminf(64.f * u * (dmax + fabsf(g.bo) + fabsf(wz) + zmax + fabsf(g.oz) +
-                                      fabsf(1.f / g.scale)) * g.inv_bw + 0.01f,
-                          1.f);
-  return tc_spans(g, tz, cl, ch, eps);
+  return tc_spans(g, tz, cl, ch, span_eps(g, ch, wz));
 }
 
 struct Points {  // measurement points [3, N] with strides
@@ -691,7 +696,7 @@ __global__ void __launch_bounds__(256) confocal_adjoint_columns_kernel(
       if (live && zn > 0 &&
           tc_bounds(dx * dx + dy * dy, wz, g.oz + ((float)za + 0.5f) / g.scale,
                     g.oz + ((float)zb + 0.5f) / g.scale, cl, ch))
-        sp = tc_spans(g, tz, cl, ch, 1.f);
+        sp = tc_spans(g, tz, cl, ch, span_eps(g, ch, wz));
       // warp union of the lanes' spans
       const int p0 = __reduce_min_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p0 : INT_MAX);
       const int p1 = __reduce_max_sync(0xffffffffu, sp.p0 <= sp.p1 ? sp.p1 : -1);
