@@ -145,8 +145,10 @@ def test_velten_bins_exact(cuda_lib, offset, origin):
 def test_velten_tiled_equals_untiled(cuda_lib):
     """The shared-memory tiled Velten kernel sums the same values in the same
     order as the one-voxel-per-thread kernel: identical volumes for 1, 2 and
-    4 voxels per thread, with registers capped (the default) or not
-    ("backprojection.velten.occupancy" = 1), and with one bin window per tile
+    4 voxels per thread, bins of two voxels at a time from paired FP32
+    instructions (the default) or one at a time ("backprojection.velten.pair"
+    = 2), with registers capped for 6 or 5 CTAs per SM or not
+    ("backprojection.velten.occupancy" = 5, 1), and with one bin window per tile
     or group windows ("backprojection.velten.groups" = 1, 2), including grids
     that are not a multiple of the voxel block. The scans cover every staging
     of a tile's bin rows (by a CPU model of the kernel's choice, for 4 voxels
@@ -167,19 +169,23 @@ def test_velten_tiled_equals_untiled(cuda_lib):
         tr = torch.from_numpy(g.random((1, T, S), dtype=np.float32)).cuda()
         sp = torch.from_numpy(pts.astype(np.float32))[None].cuda()
         out = []
-        variants = [(1, 0, 0, 0)] + [(0, vz, occ, grp) for vz, occ in ((1, 0), (2, 0), (4, 0), (4, 1))
-                                     for grp in (1, 2)]
-        for mode, vz, occ, grp in variants:
-            autotune.set_tile("backprojection.velten.mode", mode)
-            autotune.set_tile("backprojection.velten.vz", vz)
-            autotune.set_tile("backprojection.velten.occupancy", occ)
-            autotune.set_tile("backprojection.velten.groups", grp)
-            v = torch.empty((1,) + res, device="cuda")
-            K.backprojection_confocal_velten_forward(tr, sp, torch.empty((1, 0, 3), device="cuda"),
-                                                     v, (-0.5, -0.4, 0.5), (0.5, 0.45, 1.5), bw,
-                                                     0.01)
-            out.append(v)
-        for key in ("mode", "vz", "occupancy", "groups"):
-            autotune.set_tile("backprojection.velten." + key, 0)
+        keys = ("mode", "vz", "occupancy", "groups", "pair")
+        variants = [(1, 0, 0, 0, 0)] + [
+            (0, vz, occ, grp, pair)
+            for vz, occ, pair in ((1, 0, 0), (2, 0, 0), (2, 0, 2), (4, 0, 0), (4, 0, 2),
+                                  (4, 5, 0), (4, 1, 2))
+            for grp in (1, 2)]
+        try:
+            for values in variants:
+                for key, value in zip(keys, values):
+                    autotune.set_tile("backprojection.velten." + key, value)
+                v = torch.empty((1,) + res, device="cuda")
+                K.backprojection_confocal_velten_forward(
+                    tr, sp, torch.empty((1, 0, 3), device="cuda"), v, (-0.5, -0.4, 0.5),
+                    (0.5, 0.45, 1.5), bw, 0.01)
+                out.append(v)
+        finally:
+            for key in keys:
+                autotune.set_tile("backprojection.velten." + key, 0)
         for o in out[1:]:
             assert torch.equal(out[0], o)

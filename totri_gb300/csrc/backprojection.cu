@@ -109,6 +109,31 @@ __device__ __forceinline__ int velten_bin_col(fv3 q, float od2, fv3 p, float r2,
   return nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, p)))), bw, bo);
 }
 
+// velten_bin_col for two voxels of the column at once: the same operations
+// on (voxel a, voxel b) pairs with paired FP32 instructions (each rounds as
+// its scalar form), the reciprocal square roots and the decisions per voxel.
+__device__ __forceinline__ void velten_bin_col2(fv3 q, float od2, fv3 pa, fv3 pb, float r2,
+                                                float bw, float bo, float inv_bw, float nbo,
+                                                float half_m, int& ta, int& tb) {
+  const unsigned long long dz = f2sub(f2pack(q.z, q.z), f2pack(pa.z, pb.z));
+  const unsigned long long d2 = f2fma(dz, dz, f2pack(r2, r2));
+  float d2a, d2b;
+  f2unpack(d2, d2a, d2b);
+  const unsigned long long prod = f2mul(d2, f2pack(rsqrt_approx(d2a), rsqrt_approx(d2b)));
+  const unsigned long long dist = f2fma(f2pack(2.f, 2.f), prod, f2pack(od2, od2));
+  const unsigned long long v = f2fma(dist, f2pack(inv_bw, inv_bw), f2pack(nbo, nbo));
+  const unsigned long long big = f2pack(12582912.f, 12582912.f);  // 1.5 2^23
+  const unsigned long long x = f2add(v, big);
+  const unsigned long long rr = f2sub(v, f2sub(x, big));
+  float xa, xb, ra, rb;
+  f2unpack(x, xa, xb);
+  f2unpack(rr, ra, rb);
+  ta = fabsf(ra) < half_m ? __float_as_int(xa) - 0x4B400000
+                          : nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, pa)))), bw, bo);
+  tb = fabsf(rb) < half_m ? __float_as_int(xb) - 0x4B400000
+                          : nearest_bin(xadd(od2, xmul(2.f, xlen(xsub3(q, pb)))), bw, bo);
+}
+
 struct Pts3 {  // [B, n, 3] with strides
   const float* p;
   int64_t sb, sn, sc;
@@ -202,7 +227,7 @@ __device__ __forceinline__ void velten_group_stage(float* win, const int2* grp, 
 // The samples of a tile with group windows. Points j >= cnt of a partial
 // tile carry a NaN distance, whose bin (-1) is neither staged nor in [0, T):
 // they add nothing.
-template <int COLS, int STRIDE, int REGION, int VZ>
+template <int COLS, int STRIDE, int REGION, int VZ, bool kPair>
 __device__ __forceinline__ void velten_group_samples(const float* win, const float4* pts,
                                                      const int2* grp, const fv3 (&p)[VZ],
                                                      float (&value)[VZ], int cnt, int T, int S,
@@ -217,20 +242,31 @@ __device__ __forceinline__ void velten_group_samples(const float* win, const flo
       const float4 q = pts[j0 + c];
       const float dx = q.x - p[0].x, dy = q.y - p[0].y;
       const float r2 = fmaf(dx, dx, dy * dy);
-#pragma unroll
-      for (int v = 0; v < VZ; ++v) {
-        const int t = velten_bin_col(mkv(q.x, q.y, q.z), q.w, p[v], r2, bw, bo, inv_bw, nbo,
-                                     half_m);
+      auto add = [&](int v, int t) {
         const unsigned r = (unsigned)t - (unsigned)d.x;
         if (r < (unsigned)d.y) value[v] += wg[r * STRIDE + c];
         else if ((unsigned)t < (unsigned)T)
           value[v] += __ldg(trb + (size_t)t * S + s0 + j0 + c);
+      };
+      if constexpr (kPair) {
+#pragma unroll
+        for (int v = 0; v < VZ; v += 2) {
+          int ta, tb;
+          velten_bin_col2(mkv(q.x, q.y, q.z), q.w, p[v], p[v + 1], r2, bw, bo, inv_bw, nbo,
+                          half_m, ta, tb);
+          add(v, ta);
+          add(v + 1, tb);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < VZ; ++v)
+          add(v, velten_bin_col(mkv(q.x, q.y, q.z), q.w, p[v], r2, bw, bo, inv_bw, nbo, half_m));
       }
     }
   }
 }
 
-template <int VZ, int kOcc = 1, bool kGrouped = false>
+template <int VZ, int kOcc = 1, bool kGrouped = false, bool kPair = false>
 __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
     Grid g, int b, int T, int S, Pts3 sp, Pts3 so, int has_origin, float bw, float bo,
     FastBin fb, const float* __restrict__ tr, float* __restrict__ vol) {
@@ -357,32 +393,48 @@ __global__ void __launch_bounds__(256, kOcc) velten_confocal_tiled_kernel(
         const float4 q = pts[j];
         const float dx = q.x - p[0].x, dy = q.y - p[0].y;
         const float r2 = fmaf(dx, dx, dy * dy);
+        if constexpr (kPair) {
 #pragma unroll
-        for (int v = 0; v < VZ; ++v) {
-          const int t = velten_bin_col(mkv(q.x, q.y, q.z), q.w, p[v], r2, bw, bo, fb.inv_bw,
-                                       fb.nbo, half_m);
-          const unsigned r = (unsigned)t - (unsigned)tlo;
-          if (r < srows) value[v] += win[r * (kST + 1) + j];
-          else if ((unsigned)t < (unsigned)T) value[v] += __ldg(trb + (size_t)t * S + s0 + j);
+          for (int v = 0; v < VZ; v += 2) {
+            int t[2];
+            velten_bin_col2(mkv(q.x, q.y, q.z), q.w, p[v], p[v + 1], r2, bw, bo, fb.inv_bw,
+                            fb.nbo, half_m, t[0], t[1]);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const unsigned r = (unsigned)t[h] - (unsigned)tlo;
+              if (r < srows) value[v + h] += win[r * (kST + 1) + j];
+              else if ((unsigned)t[h] < (unsigned)T)
+                value[v + h] += __ldg(trb + (size_t)t[h] * S + s0 + j);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < VZ; ++v) {
+            const int t = velten_bin_col(mkv(q.x, q.y, q.z), q.w, p[v], r2, bw, bo, fb.inv_bw,
+                                         fb.nbo, half_m);
+            const unsigned r = (unsigned)t - (unsigned)tlo;
+            if (r < srows) value[v] += win[r * (kST + 1) + j];
+            else if ((unsigned)t < (unsigned)T) value[v] += __ldg(trb + (size_t)t * S + s0 + j);
+          }
         }
       }
     } else if (cols == 8) {
       velten_group_stage<8, 9, 2088>(win, grp, cnt, tile_rows, trb, S, s0);
       __syncthreads();
       const float half_m = 0.5f - tile_margin;
-      velten_group_samples<8, 9, 2088>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+      velten_group_samples<8, 9, 2088, VZ, kPair>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
                                        fb.nbo, half_m, trb);
     } else if (cols == 4) {
       velten_group_stage<4, 5, 1028>(win, grp, cnt, tile_rows, trb, S, s0);
       __syncthreads();
       const float half_m = 0.5f - tile_margin;
-      velten_group_samples<4, 5, 1028>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+      velten_group_samples<4, 5, 1028, VZ, kPair>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
                                        fb.nbo, half_m, trb);
     } else {
       velten_group_stage<1, 1, 257>(win, grp, cnt, tile_rows, trb, S, s0);
       __syncthreads();
       const float half_m = 0.5f - tile_margin;
-      velten_group_samples<1, 1, 257>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
+      velten_group_samples<1, 1, 257, VZ, kPair>(win, pts, grp, p, value, cnt, T, S, s0, bw, bo, fb.inv_bw,
                                       fb.nbo, half_m, trb);
     }
   }
@@ -624,22 +676,33 @@ int totri_backprojection_confocal_velten_forward(const totri_array_t* transient,
     // spills; 34 KB of shared memory each): 38.2 ms against 40.4 ms uncapped
     // (47 registers, 5 CTAs; "backprojection.velten.occupancy" = 1), the same
     // volume bit for bit.
-#define TOTRI_VELTEN_TILED(VZ, OCC)                                                        \
+#define TOTRI_VELTEN_TILED(VZ, OCC, PAIR)                                                  \
   TOTRI_KERNEL("backprojection velten confocal", stream,                                  \
-               grouped ? (bp::velten_confocal_tiled_kernel<VZ, OCC, true>                 \
+               grouped ? (bp::velten_confocal_tiled_kernel<VZ, OCC, true, PAIR>           \
                           <<<grid, 256, 0, stream>>>(g, b, T, (int)S, sp, so, So > 0, bw, \
                                                      bo, fb, trp, volp))                  \
-                       : (bp::velten_confocal_tiled_kernel<VZ, OCC, false>                \
+                       : (bp::velten_confocal_tiled_kernel<VZ, OCC, false, PAIR>          \
                           <<<grid, 256, 0, stream>>>(g, b, T, (int)S, sp, so, So > 0, bw, \
                                                      bo, fb, trp, volp)))
-    if (tiled && vz == 4 && tune::get("backprojection.velten.occupancy") != 1)
-      TOTRI_VELTEN_TILED(4, 6);
+    // Bins of two voxels at a time with paired FP32 instructions
+    // (velten_bin_col2; "backprojection.velten.pair" = 2 takes them one at a
+    // time): 33.3 ms against 39.0 ms, the same volume bit for bit.
+    const bool pair = tune::get("backprojection.velten.pair") != 2;
+    const int occ = (int)tune::get("backprojection.velten.occupancy");
+    if (tiled && vz == 4 && pair && occ == 5)
+      TOTRI_VELTEN_TILED(4, 5, true);
+    else if (tiled && vz == 4 && pair && occ != 1)
+      TOTRI_VELTEN_TILED(4, 6, true);
+    else if (tiled && vz == 4 && occ != 1)
+      TOTRI_VELTEN_TILED(4, 6, false);
     else if (tiled && vz == 4)
-      TOTRI_VELTEN_TILED(4, 1);
+      TOTRI_VELTEN_TILED(4, 1, false);
+    else if (tiled && vz == 2 && pair)
+      TOTRI_VELTEN_TILED(2, 1, true);
     else if (tiled && vz == 2)
-      TOTRI_VELTEN_TILED(2, 1);
+      TOTRI_VELTEN_TILED(2, 1, false);
     else if (tiled)
-      TOTRI_VELTEN_TILED(1, 1);
+      TOTRI_VELTEN_TILED(1, 1, false);
 #undef TOTRI_VELTEN_TILED
     else
       TOTRI_KERNEL("backprojection velten confocal", stream,
