@@ -31,10 +31,11 @@
 //   "volume.adjoint.warps"      warps per CTA of the lanes-over-columns adjoint
 //   "volume.adjoint.slabs"      z slabs of its columns (default: slabs of <= 64 cells)
 //   "volume.exhaustive.lt"      laser points per exhaustive volume CTA (1,8,32)
-//   "backprojection.velten.mode", ".occupancy", ".vz", ".groups"
-//                               Velten kernel variant, 1: uncapped registers, slab depth,
-//                               bin windows (1 one per tile, 2 per point group; 0: by the
-//                               voxel block's span in bins)
+//   "backprojection.velten.mode", ".occupancy", ".vz", ".groups", ".pair"
+//                               Velten kernel variant, 1: uncapped registers (5: capped for
+//                               5 CTAs per SM), slab depth, bin windows (1 one per tile, 2 per
+//                               point group; 0: by the voxel block's span in bins), 2: bins
+//                               one voxel at a time instead of paired
 //   "rbf.cull"                  1: RBF kernels without the underflow cull
 #pragma once
 
