@@ -83,8 +83,9 @@ def test_underflow_cull_is_bit_identical(cuda_lib, attrs):
     """Gaussians whose ex2 value underflows to zero over a whole voxel brick
     are skipped; the forward stays bit for bit the same (zero terms, same
     order), also with non-finite and degenerate Gaussians in the set and a
-    grid that does not divide into bricks, and the gradient (summed with
-    atomics, so only equal up to their order) agrees to FP32 rounding."""
+    grid that does not divide into bricks, and with one voxel per thread
+    instead of two ("rbf.forward.vz" = 1); the gradient (summed with atomics,
+    so only equal up to their order) agrees to FP32 rounding."""
     from totri_gb300.totri_cpp import util as U
     rng = np.random.default_rng(40 + attrs)
     N = 700
@@ -107,6 +108,15 @@ def test_underflow_cull_is_bit_identical(cuda_lib, attrs):
     on, off = fwd(), _with_cull(True, fwd)
     assert torch.equal(torch.nan_to_num(on, nan=1234.5), torch.nan_to_num(off, nan=1234.5))
     assert torch.equal(torch.isnan(on), torch.isnan(off))
+    # one voxel per thread instead of two (paired FP32): the same bits
+    from totri_gb300 import autotune
+    autotune.set_tile("rbf.forward.vz", 1)
+    try:
+        one = fwd()
+    finally:
+        autotune.set_tile("rbf.forward.vz", 0)
+    assert torch.equal(torch.nan_to_num(on, nan=1234.5), torch.nan_to_num(one, nan=1234.5))
+    assert torch.equal(torch.isnan(on), torch.isnan(one))
 
     ok = np.isfinite(rbf).all(1) & (rbf[:, 3] > 0)  # the gradient on finite Gaussians
     r = torch.as_tensor(rbf[ok][None]).cuda()

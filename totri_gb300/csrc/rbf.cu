@@ -104,6 +104,11 @@ __device__ __forceinline__ int block_slot(bool flag, int* warp_counts, int* tota
 // Forward: a CTA per brick of 8 x 8 x 4 voxels (x fastest), one thread per
 // voxel; Gaussians come in tiles of 256, each culled against the brick's box,
 // and the survivors are evaluated in their original order.
+// VZ voxels of a column per thread, 4 apart in z (bricks of 8 x 8 x 4 VZ).
+// With VZ = 2 the two voxels share the Gaussian's loads and dx, dy, and their
+// exponents and sums run as paired FP32 instructions (each rounds as its
+// scalar form, in the same order), so the volume is the same bit for bit.
+template <int VZ>
 __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int N, int C, int cull,
                                                       float* __restrict__ vol) {
   __shared__ float tile[kTile][4 + kMaxAttr];
@@ -111,19 +116,30 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
   const int A = C - 4;
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   const int tid = threadIdx.x;
-  const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 4;
-  const int xi = bx + (tid & 7), yi = by + ((tid >> 3) & 7), zi = bz + (tid >> 6);
-  const bool inside = xi < g.W && yi < g.H && zi < g.D;
+  const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 4 * VZ;
+  const int xi = bx + (tid & 7), yi = by + ((tid >> 3) & 7);
+  int zi[VZ];
+  bool inside[VZ];
+  float z[VZ];
+#pragma unroll
+  for (int v = 0; v < VZ; ++v) {
+    zi[v] = bz + (tid >> 6) + 4 * v;
+    inside[v] = xi < g.W && yi < g.H && zi[v] < g.D;
+    z[v] = coord(g.sz, g.ez, g.D, zi[v]);
+  }
   const float x = coord(g.sx, g.ex, g.W, xi), y = coord(g.sy, g.ey, g.H, yi);
-  const float z = coord(g.sz, g.ez, g.D, zi);
   float lo[3], hi[3];
   axis_box(g.sx, g.ex, g.W, bx, min(bx + 7, g.W - 1), lo[0], hi[0]);
   axis_box(g.sy, g.ey, g.H, by, min(by + 7, g.H - 1), lo[1], hi[1]);
-  axis_box(g.sz, g.ez, g.D, bz, min(bz + 3, g.D - 1), lo[2], hi[2]);
-  float sum = 0.f;
-  float attr[kMaxAttr];
+  axis_box(g.sz, g.ez, g.D, bz, min(bz + 4 * VZ - 1, g.D - 1), lo[2], hi[2]);
+  float sum[VZ];
+  float attr[VZ][kMaxAttr];
 #pragma unroll
-  for (int a = 0; a < kMaxAttr; ++a) attr[a] = 0.f;
+  for (int v = 0; v < VZ; ++v) {
+    sum[v] = 0.f;
+#pragma unroll
+    for (int a = 0; a < kMaxAttr; ++a) attr[v][a] = 0.f;
+  }
   for (int i0 = 0; i0 < N; i0 += kTile) {
     __syncthreads();  // the previous tile has been read
     float val[4 + kMaxAttr];
@@ -145,22 +161,46 @@ __global__ void __launch_bounds__(256) forward_kernel(Grid g, int b, Rbf r, int 
       for (int c = 0; c < C; ++c) tile[at][c] = val[c];
     __syncthreads();
     for (int i = 0; i < cnt; ++i) {
-      const float dx = tile[i][0] - x, dy = tile[i][1] - y, dz = tile[i][2] - z;
-      const float w = exp2_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * tile[i][3]);
-      sum += w;
+      const float dx = tile[i][0] - x, dy = tile[i][1] - y;
+      if constexpr (VZ == 2) {
+        const unsigned long long dz = f2sub(f2pack(tile[i][2], tile[i][2]), f2pack(z[0], z[1]));
+        const unsigned long long d2 =
+            f2fma(f2pack(dx, dx), f2pack(dx, dx),
+                  f2fma(f2pack(dy, dy), f2pack(dy, dy), f2mul(dz, dz)));
+        float e0, e1;
+        f2unpack(f2mul(d2, f2pack(tile[i][3], tile[i][3])), e0, e1);
+        const unsigned long long w = f2pack(exp2_approx(e0), exp2_approx(e1));
+        unsigned long long s2 = f2add(f2pack(sum[0], sum[1]), w);
+        f2unpack(s2, sum[0], sum[1]);
 #pragma unroll
-      for (int a = 0; a < kMaxAttr; ++a)
-        if (a < A) attr[a] += w * tile[i][4 + a];
+        for (int a = 0; a < kMaxAttr; ++a)
+          if (a < A) {
+            const float t = tile[i][4 + a];
+            f2unpack(f2fma(w, f2pack(t, t), f2pack(attr[0][a], attr[1][a])), attr[0][a],
+                     attr[1][a]);
+          }
+      } else {
+        const float dz = tile[i][2] - z[0];
+        const float w = exp2_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * tile[i][3]);
+        sum[0] += w;
+#pragma unroll
+        for (int a = 0; a < kMaxAttr; ++a)
+          if (a < A) attr[0][a] = fmaf(w, tile[i][4 + a], attr[0][a]);
+      }
     }
   }
-  if (!inside) return;
-  const int64_t v = ((int64_t)zi * g.H + yi) * g.W + xi;
-  float* out = vol + (size_t)b * (1 + A) * nv;
-  out[v] = sum;
-  const float norm = sum < 1e-8f ? 1.f : sum;
+  const int A1 = A;
+  float* out = vol + (size_t)b * (1 + A1) * nv;
 #pragma unroll
-  for (int a = 0; a < kMaxAttr; ++a)
-    if (a < A) out[(size_t)(1 + a) * nv + v] = attr[a] / norm;
+  for (int v = 0; v < VZ; ++v) {
+    if (!inside[v]) continue;
+    const int64_t o = ((int64_t)zi[v] * g.H + yi) * g.W + xi;
+    out[o] = sum[v];
+    const float norm = sum[v] < 1e-8f ? 1.f : sum[v];
+#pragma unroll
+    for (int a = 0; a < kMaxAttr; ++a)
+      if (a < A1) out[(size_t)(1 + a) * nv + o] = attr[v][a] / norm;
+  }
 }
 
 constexpr int kChunk = 512;  // voxels of a gradient brick (8 x 8 x 8)
@@ -332,11 +372,20 @@ int totri_rbf2volume_gaussian_forward(const totri_array_t* r, const totri_array_
   const int64_t nv = (int64_t)g.D * g.H * g.W;
   if (nv == 0 || B == 0) return TOTRI_OK;
   const int cull = tune::get("rbf.cull") != 1;
-  const dim3 grid((unsigned)ceil_div(g.W, 8), (unsigned)ceil_div(g.H, 8), (unsigned)ceil_div(g.D, 4));
-  for (int b = 0; b < (int)B; ++b)
-    TOTRI_KERNEL("rbf2volume forward", stream,
-                 rbf::forward_kernel<<<grid, 256, 0, stream>>>(g, b, rr, (int)N, C, cull,
-                                                               static_cast<float*>(vol->data)));
+  // two voxels per thread ("rbf.forward.vz" = 1: one)
+  const int vz = tune::get("rbf.forward.vz") == 1 ? 1 : 2;
+  const dim3 grid((unsigned)ceil_div(g.W, 8), (unsigned)ceil_div(g.H, 8),
+                  (unsigned)ceil_div(g.D, 4 * vz));
+  for (int b = 0; b < (int)B; ++b) {
+    if (vz == 2)
+      TOTRI_KERNEL("rbf2volume forward", stream,
+                   rbf::forward_kernel<2><<<grid, 256, 0, stream>>>(
+                       g, b, rr, (int)N, C, cull, static_cast<float*>(vol->data)));
+    else
+      TOTRI_KERNEL("rbf2volume forward", stream,
+                   rbf::forward_kernel<1><<<grid, 256, 0, stream>>>(
+                       g, b, rr, (int)N, C, cull, static_cast<float*>(vol->data)));
+  }
   return TOTRI_OK;
 }
 

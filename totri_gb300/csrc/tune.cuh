@@ -37,6 +37,7 @@
 //                               point group; 0: by the voxel block's span in bins), 2: bins
 //                               one voxel at a time instead of paired
 //   "rbf.cull"                  1: RBF kernels without the underflow cull
+//   "rbf.forward.vz"            1: one voxel per thread in the RBF forward (default two)
 #pragma once
 
 #include <cuda_runtime.h>
