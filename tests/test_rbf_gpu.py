@@ -130,3 +130,10 @@ def test_underflow_cull_is_bit_identical(cuda_lib, attrs):
 
     g_on, g_off = grad(), _with_cull(True, grad)
     assert rel(g_on.cpu().numpy(), g_off.cpu().numpy()) < 1e-6
+    # one Gaussian per warp iteration instead of two (paired FP32)
+    autotune.set_tile("rbf.grad.pair", 2)
+    try:
+        g_one = grad()
+    finally:
+        autotune.set_tile("rbf.grad.pair", 0)
+    assert rel(g_on.cpu().numpy(), g_one.cpu().numpy()) < 1e-6

@@ -330,6 +330,139 @@ __global__ void __launch_bounds__(256) grad_kernel(Grid g, int b, Rbf r, int N, 
   }
 }
 
+
+// grad_kernel with two Gaussians per warp iteration: each staged voxel
+// record is read once for both, the voxel's 1 / vol[0] is shared, and the
+// two Gaussians' terms run as paired FP32 instructions (the ex2 per
+// Gaussian). kA attributes at most (1 or kMaxAttr): fewer live registers for
+// the common single weight.
+template <int kA>
+__global__ void __launch_bounds__(256) grad_pair_kernel(Grid g, int b, Rbf r, int N, int C,
+                                                        int cull, const float* __restrict__ vol,
+                                                        const float* __restrict__ vgrad,
+                                                        float* __restrict__ rgrad, int64_t gsb,
+                                                        int64_t gsn, int64_t gsc) {
+  using u64 = unsigned long long;
+  extern __shared__ float sm[];
+  __shared__ int list[kTile];
+  __shared__ int counts[8];
+  const int A = C - 4;
+  const int stride = grad_stride(A);
+  const int64_t nv = (int64_t)g.D * g.H * g.W;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int bx = blockIdx.x * 8, by = blockIdx.y * 8, bz = blockIdx.z * 8;
+  const float* vb = vol + (size_t)b * (1 + A) * nv;
+  const float* gb = vgrad + (size_t)b * (1 + A) * nv;
+  for (int j = tid; j < kChunk; j += blockDim.x) {
+    const int xi = bx + (j & 7), yi = by + ((j >> 3) & 7), zi = bz + (j >> 6);
+    float* e = sm + j * stride;
+    const bool in = xi < g.W && yi < g.H && zi < g.D;
+    e[0] = coord(g.sx, g.ex, g.W, xi);
+    e[1] = coord(g.sy, g.ey, g.H, yi);
+    e[2] = coord(g.sz, g.ez, g.D, zi);
+    e[3] = in ? 1.f : 0.f;
+    const int64_t v = in ? ((int64_t)zi * g.H + yi) * g.W + xi : 0;
+    for (int q = 0; q <= A; ++q) {
+      e[4 + q] = in ? vb[(size_t)q * nv + v] : 0.f;
+      e[4 + 1 + A + q] = in ? gb[(size_t)q * nv + v] : 0.f;
+    }
+  }
+  float lo[3], hi[3];
+  axis_box(g.sx, g.ex, g.W, bx, min(bx + 7, g.W - 1), lo[0], hi[0]);
+  axis_box(g.sy, g.ey, g.H, by, min(by + 7, g.H - 1), lo[1], hi[1]);
+  axis_box(g.sz, g.ez, g.D, bz, min(bz + 7, g.D - 1), lo[2], hi[2]);
+  for (int i0 = 0; i0 < N; i0 += kTile) {
+    __syncthreads();  // the staged voxels are written / the previous list is read
+    bool keep = false;
+    if (i0 + tid < N) {
+      const float cx = r.at(b, i0 + tid, 0), cy = r.at(b, i0 + tid, 1);
+      const float cz = r.at(b, i0 + tid, 2), sg = r.at(b, i0 + tid, 3);
+      const float k2 = -0.5f * kLog2e * (1.f / (sg * sg));
+      keep = !cull || !(isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(k2)) ||
+             !(box_dist2(cx, cy, cz, lo, hi) * -k2 > kCullArg);
+    }
+    int cnt;
+    const int at = block_slot(keep, counts, &cnt);
+    if (keep) list[at] = i0 + tid;
+    __syncthreads();
+    for (int q = 2 * warp; q < cnt; q += 16) {
+      const bool two = q + 1 < cnt;
+      const int ia = list[q], ib = two ? list[q + 1] : ia;
+      float sga = r.at(b, ia, 3), sgb = r.at(b, ib, 3);
+      const float is2a = 1.f / (sga * sga), is2b = 1.f / (sgb * sgb);
+      const u64 XR = f2pack(r.at(b, ia, 0), r.at(b, ib, 0));
+      const u64 YR = f2pack(r.at(b, ia, 1), r.at(b, ib, 1));
+      const u64 ZR = f2pack(r.at(b, ia, 2), r.at(b, ib, 2));
+      const u64 IS2 = f2pack(is2a, is2b);
+      const u64 K2 = f2pack(-0.5f * kLog2e * is2a, -0.5f * kLog2e * is2b);
+      const u64 IS3 = f2pack(is2a / sga, is2b / sgb);
+      u64 RA[kA];
+#pragma unroll
+      for (int a = 0; a < kA; ++a)
+        RA[a] = a < A ? f2pack(r.at(b, ia, 4 + a), r.at(b, ib, 4 + a)) : 0ull;
+      u64 GX = 0ull, GY = 0ull, GZ = 0ull, GS = 0ull;  // (+0, +0)
+      u64 GA[kA];
+#pragma unroll
+      for (int a = 0; a < kA; ++a) GA[a] = 0ull;
+      for (int j = lane; j < kChunk; j += 32) {
+        const float* e = sm + j * stride;
+        if (e[3] == 0.f) continue;  // outside the grid
+        const u64 EX = f2sub(f2pack(e[0], e[0]), XR);
+        const u64 EY = f2sub(f2pack(e[1], e[1]), YR);
+        const u64 EZ = f2sub(f2pack(e[2], e[2]), ZR);
+        const u64 D2 = f2fma(EX, EX, f2fma(EY, EY, f2mul(EZ, EZ)));
+        float ta, tb;
+        f2unpack(f2mul(D2, K2), ta, tb);
+        const u64 W = f2pack(exp2_approx(ta), exp2_approx(tb));
+        const u64 WI = f2mul(IS2, W);
+        const u64 DWS = f2mul(f2mul(D2, IS3), W);
+        const float dl0 = e[4 + 1 + A];
+        u64 DL = f2pack(dl0, dl0);
+        if (A > 0) {
+          float v0 = e[4];
+          if (v0 < 1e-8f) v0 = 1.f;
+          const float inv = 1.f / v0;
+          const u64 INV = f2pack(inv, inv);
+          u64 S = 0ull;
+#pragma unroll
+          for (int a = 0; a < kA; ++a) {
+            if (a < A) {
+              const float dla = e[4 + 1 + A + 1 + a], ea = e[4 + 1 + a];
+              const u64 DLA = f2pack(dla, dla);
+              S = f2fma(DLA, f2sub(RA[a], f2pack(ea, ea)), S);
+              GA[a] = f2fma(f2mul(DLA, W), INV, GA[a]);
+            }
+          }
+          DL = f2fma(S, INV, DL);
+        }
+        GX = f2fma(f2mul(EX, WI), DL, GX);
+        GY = f2fma(f2mul(EY, WI), DL, GY);
+        GZ = f2fma(f2mul(EZ, WI), DL, GZ);
+        GS = f2fma(DWS, DL, GS);
+      }
+      float out2[2][4 + kA];
+      f2unpack(GX, out2[0][0], out2[1][0]);
+      f2unpack(GY, out2[0][1], out2[1][1]);
+      f2unpack(GZ, out2[0][2], out2[1][2]);
+      f2unpack(GS, out2[0][3], out2[1][3]);
+#pragma unroll
+      for (int a = 0; a < kA; ++a) f2unpack(GA[a], out2[0][4 + a], out2[1][4 + a]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int c = 0; c < 4 + kA; ++c)
+          if (c < 4 + A) out2[h][c] = warp_sum_f(out2[h][c]);
+        if (lane == 0 && (h == 0 || two)) {
+          float* o = rgrad + b * gsb + (h ? ib : ia) * gsn;
+#pragma unroll
+          for (int c = 0; c < 4 + kA; ++c)
+            if (c < 4 + A) atomicAdd(o + c * gsc, out2[h][c]);
+        }
+      }
+    }
+  }
+}
+
 }  // namespace rbf
 
 namespace {
@@ -411,16 +544,34 @@ int totri_rbf2volume_gaussian_grad(const totri_array_t* r, const totri_array_t* 
   if (nv == 0 || N == 0 || B == 0) return TOTRI_OK;
   const int A = C - 4;
   const size_t smem = sizeof(float) * rbf::kChunk * rbf::grad_stride(A);
-  TOTRI_CUDA(tune::ensure_dynamic_smem(
-      reinterpret_cast<const void*>(rbf::grad_kernel), smem));
   const int cull = tune::get("rbf.cull") != 1;
   const dim3 grid((unsigned)ceil_div(g.W, 8), (unsigned)ceil_div(g.H, 8), (unsigned)ceil_div(g.D, 8));
-  for (int b = 0; b < (int)B; ++b)
-    TOTRI_KERNEL("rbf2volume grad", stream,
-                 rbf::grad_kernel<<<grid, 256, smem, stream>>>(
-                     g, b, rr, (int)N, C, cull, static_cast<const float*>(vol->data),
-                     static_cast<const float*>(vgrad->data), static_cast<float*>(rgrad->data),
-                     rgrad->strides[0], rgrad->strides[1], rgrad->strides[2]));
+  // two Gaussians per warp iteration ("rbf.grad.pair" = 2: one)
+  const bool pair = tune::get("rbf.grad.pair") != 2;
+  const void* fn = !pair ? reinterpret_cast<const void*>(rbf::grad_kernel)
+                   : A <= 1 ? reinterpret_cast<const void*>(rbf::grad_pair_kernel<1>)
+                            : reinterpret_cast<const void*>(rbf::grad_pair_kernel<rbf::kMaxAttr>);
+  TOTRI_CUDA(tune::ensure_dynamic_smem(fn, smem));
+  const float* vp = static_cast<const float*>(vol->data);
+  const float* gp = static_cast<const float*>(vgrad->data);
+  float* rp = static_cast<float*>(rgrad->data);
+  for (int b = 0; b < (int)B; ++b) {
+    if (!pair)
+      TOTRI_KERNEL("rbf2volume grad", stream,
+                   rbf::grad_kernel<<<grid, 256, smem, stream>>>(
+                       g, b, rr, (int)N, C, cull, vp, gp, rp, rgrad->strides[0],
+                       rgrad->strides[1], rgrad->strides[2]));
+    else if (A <= 1)
+      TOTRI_KERNEL("rbf2volume grad", stream,
+                   rbf::grad_pair_kernel<1><<<grid, 256, smem, stream>>>(
+                       g, b, rr, (int)N, C, cull, vp, gp, rp, rgrad->strides[0],
+                       rgrad->strides[1], rgrad->strides[2]));
+    else
+      TOTRI_KERNEL("rbf2volume grad", stream,
+                   rbf::grad_pair_kernel<rbf::kMaxAttr><<<grid, 256, smem, stream>>>(
+                       g, b, rr, (int)N, C, cull, vp, gp, rp, rgrad->strides[0],
+                       rgrad->strides[1], rgrad->strides[2]));
+  }
   return TOTRI_OK;
 }
 

@@ -38,6 +38,8 @@
 //                               one voxel at a time instead of paired
 //   "rbf.cull"                  1: RBF kernels without the underflow cull
 //   "rbf.forward.vz"            1: one voxel per thread in the RBF forward (default two)
+//   "rbf.grad.pair"             2: one Gaussian per warp iteration in the RBF gradient
+//                               (default two)
 #pragma once
 
 #include <cuda_runtime.h>
