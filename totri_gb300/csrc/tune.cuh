@@ -17,6 +17,9 @@
 //                               registers) instead of 3
 //   "mesh.exhaustive.grad.lchunk", ".sslice" lasers / scan points per CTA of the
 //                               point-record gradient (at most 256 each)
+//   "mesh.exhaustive.grad.layout" 2: read transient_grad in place even when the
+//                               workspace holds the bins-last scratch
+//   "mesh.exhaustive.grad.chunk" most scan points per bins-last copy
 //   "mesh.exhaustive.grad.split" scan-point slices per exhaustive gradient chunk
 //   "mesh.visibility.mode"      1 per-lane BVH walk, 2 warp-packet walk, 7 one hull
 //                               per target (at its launcher)
