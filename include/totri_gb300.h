@@ -287,7 +287,9 @@ int totri_mesh_prepared_confocal_grad_verts(
 
 /* Scratch bytes for the volume entry points that list occupied voxels
  * (confocal forward, measurement-point gradient, exhaustive forward):
- * num_voxels = X*Y*Z (or D*H*W of one batch item). */
+ * num_voxels = X*Y*Z (or D*H*W of one batch item). A 256-byte header, then
+ * 16 bytes per voxel (the confocal entry points keep one record per occupied
+ * voxel: column centre, value and cell). */
 size_t totri_volume_workspace(int64_t num_voxels);
 
 /* Replaces totri_cpp.render.volume_confocal_forward
